@@ -1,0 +1,359 @@
+"""Benchmark of the Hashinator hot path on GB300.
+
+Workload (one step): the large single-map configuration with 32-bit keys and
+values — clear a table of 2^27 buckets, insert 2^26 distinct keys (load
+factor 0.5), then retrieve 2^26 queries of which half are present and half
+absent. Metric: insert + query throughput in Mkeys/s (2 x 2^26 keys per step).
+The table (1 GiB) and key arrays (256 MiB each) are larger than L2 (129 MB),
+so no L2 flush is needed between steps.
+
+value: device-resident inputs, CUDA events around the K timed steps.
+e2e:   the same step through the C ABI with pinned HOST buffers: the H2D copy
+       of keys, values and queries and the D2H copy of the query results are
+       inside the timed region.
+roofline: the dominant kernel's algorithmic bytes (insert 72 B/key, query
+       40 B/key: key+value in, one 32 B bucket sector read, written back for
+       insert) over its event-timed duration, against the measured HBM copy
+       bandwidth (MEASURED_PEAKS.json).
+cpu_baseline: the oracle's serial C restatement on a bounded sample
+       (2^24 keys into 2^25 buckets, same load factor), one host core.
+
+--impl reference times the reference's CPU implementation of the path (the
+oracle port of it on this machine) on the same metric.
+Multi-GPU: replicas only (each rank runs the same single-map workload on its
+own GPU; value is the sum over ranks).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SP = 27
+N_KEYS = 1 << 26
+INSERT_BYTES_PER_KEY = {4: 72, 8: 80}
+QUERY_BYTES_PER_KEY = {4: 40, 8: 48}
+METRIC = "insert+query Mkeys/s (u32 keys/values, 2^26 keys, 2^27 buckets, LF 0.5, 50% hit queries)"
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel_tag: str):
+    """Per-launch DRAM bytes of a kernel from profiles/roofline_traffic.md
+    (lines of the form `traffic <tag> <bytes>`), or None."""
+    p = ROOT / "profiles" / "roofline_traffic.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        parts = line.strip().strip("`").split()
+        if len(parts) == 3 and parts[0] == "traffic" and parts[1] == kernel_tag:
+            try:
+                return float(parts[2])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline(width: int = 4, log_n: int = 24):
+    """Oracle port on a bounded sample: insert + 50/50 query, 1 core."""
+    import oracle
+    from hashinator_gb300 import workloads
+    n = 1 << log_n
+    keys, vals, q, _ = workloads.map_workload(n, width, 1234, erase_frac=0.0)
+    om = oracle.OracleMap(log_n + 1, width)
+    out = np.zeros(len(q), keys.dtype)
+    t0 = time.perf_counter()
+    om.insert(keys, vals, 0.0)
+    t1 = time.perf_counter()
+    om.retrieve(q, out)
+    t2 = time.perf_counter()
+    total = t2 - t0
+    return {"value": round(2 * n / total / 1e6, 3), "unit": "Mkeys/s", "cores": 1, "kind": "port",
+            "sample": f"2^{log_n} u32 keys into 2^{log_n + 1} buckets (LF 0.5) + 2^{log_n} queries 50% hit; "
+                      f"insert {n / (t1 - t0) / 1e6:.1f} Mkeys/s, query {n / (t2 - t1) / 1e6:.1f} Mkeys/s",
+            "seconds": round(total, 3)}
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    import oracle  # the reference's CPU path, restated (no build of the reference exists on this machine)
+    from hashinator_gb300 import workloads
+    log_n = 22
+    n = 1 << log_n
+    keys, vals, q, _ = workloads.map_workload(n, 4, 1234, erase_frac=0.0)
+    out = np.zeros(len(q), keys.dtype)
+    times = []
+    for i in range(args.warmup + args.steps):
+        om = oracle.OracleMap(log_n + 1, 4)
+        t0 = time.perf_counter()
+        om.insert(keys, vals, 0.0)
+        om.retrieve(q, out)
+        dt = time.perf_counter() - t0
+        del om
+        if i >= args.warmup:
+            times.append(dt)
+    t = float(np.mean(times))
+    v = 2 * n / t / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "Mkeys/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded bijective keys)",
+            "config": {"workload": "single map u32/u32, insert + 50/50 query, LF 0.5",
+                       "sample": f"2^{log_n} keys into 2^{log_n + 1} buckets per step", "parallelism": "none"},
+            "cpu_baseline": {"value": round(v, 3), "unit": "Mkeys/s", "cores": 1, "kind": "port",
+                             "sample": f"2^{log_n} keys, 2^{log_n + 1} buckets, insert + 2^{log_n} queries 50% hit"},
+            "e2e": {"value": round(v, 3), "unit": "Mkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import hashinator_gb300 as hx
+    from hashinator_gb300 import workloads
+
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    hx.lib()
+    width = 4
+    n = N_KEYS
+    keys, vals, q, _ = workloads.map_workload(n, width, 2026 + rank, erase_frac=0.0)
+
+    def to_dev(a):
+        return torch.from_numpy(a.view(np.int32)).to(dev)
+
+    d_keys, d_vals, d_q = to_dev(keys), to_dev(vals), to_dev(q)
+    d_out = torch.empty(n, dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    m = hx.Hashmap(SP, width, stream=stream)
+    if args.group:
+        m.set_tuning(group_width=args.group)
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        m.clear(stream=stream)
+        if ev:
+            ev[1].record(stream)
+        m.insert(d_keys, d_vals, target_lf=0.5, stream=stream)
+        if ev:
+            ev[2].record(stream)
+        m.retrieve(d_q, d_out, stream=stream)
+        if ev:
+            ev[3].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # correctness spot check of the last step (not timed)
+    host_out = d_out.cpu().numpy().view(np.uint32)
+    present = np.isin(q[:4096], keys)
+    assert present.sum() > 0
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    l0 = hx.kernel_launch_count()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for i in range(args.steps):
+        step(evs[i])
+    stop.record(stream)
+    torch.cuda.synchronize()
+    launches = hx.kernel_launch_count() - l0
+    elapsed = start.elapsed_time(stop) / 1e3
+    if world > 1:
+        t = torch.tensor([elapsed], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t.item())
+    clocks = sampler.stop()
+    t_clear = float(np.mean([e[0].elapsed_time(e[1]) for e in evs])) / 1e3
+    t_ins = float(np.mean([e[1].elapsed_time(e[2]) for e in evs])) / 1e3
+    t_q = float(np.mean([e[2].elapsed_time(e[3]) for e in evs])) / 1e3
+    ms_per_step = elapsed / args.steps * 1e3
+    value = world * 2 * n * args.steps / elapsed / 1e6
+
+    # ---- end-to-end through the C ABI with pinned host buffers ----------
+    e2e = None
+    if not args.no_e2e:
+        h_keys = torch.from_numpy(keys.view(np.int32)).pin_memory()
+        h_vals = torch.from_numpy(vals.view(np.int32)).pin_memory()
+        h_q = torch.from_numpy(q.view(np.int32)).pin_memory()
+        h_out = torch.empty(n, dtype=torch.int32).pin_memory()
+
+        def e2e_step():
+            with torch.cuda.stream(stream):
+                d_keys.copy_(h_keys, non_blocking=True)
+                d_vals.copy_(h_vals, non_blocking=True)
+                d_q.copy_(h_q, non_blocking=True)
+            m.clear(stream=stream)
+            m.insert(d_keys, d_vals, target_lf=0.5, stream=stream)
+            m.retrieve(d_q, d_out, stream=stream)
+            with torch.cuda.stream(stream):
+                h_out.copy_(d_out, non_blocking=True)
+
+        for _ in range(max(1, args.warmup // 2)):
+            e2e_step()
+        torch.cuda.synchronize()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        s1.record(stream)
+        torch.cuda.synchronize()
+        e_el = s0.elapsed_time(s1) / 1e3
+        if world > 1:
+            t = torch.tensor([e_el], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e_el = float(t.item())
+        # result check of the e2e output against the device-timed output
+        assert np.array_equal(h_out.numpy().view(np.uint32)[:65536], host_out[:65536])
+        e2e = {"value": round(world * 2 * n * args.steps / e_el / 1e6, 3), "unit": "Mkeys/s",
+               "h2d_bytes_per_step": 3 * n * width, "d2h_bytes_per_step": n * width,
+               "ms_per_step": round(e_el / args.steps * 1e3, 3)}
+
+    peak, peak_kind = measured_peak()
+    ins_gbs = INSERT_BYTES_PER_KEY[width] * n / t_ins / 1e9
+    q_gbs = QUERY_BYTES_PER_KEY[width] * n / t_q / 1e9
+    dominant = "insert" if t_ins >= t_q else "query"
+    achieved = ins_gbs if dominant == "insert" else q_gbs
+    traffic = traffic_from_profiles(f"{dominant}_u32_lf050")
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
+                "kernel": f"k_insert (insert)" if dominant == "insert" else "k_retrieve (query)",
+                "algorithmic_bytes_per_launch": (INSERT_BYTES_PER_KEY if dominant == "insert"
+                                                 else QUERY_BYTES_PER_KEY)[width] * n,
+                "per_op": {"insert": {"ms": round(t_ins * 1e3, 3), "Mkeys_s": round(n / t_ins / 1e6, 1),
+                                      "GB_s": round(ins_gbs, 1), "frac": round(ins_gbs / peak, 4)},
+                           "query": {"ms": round(t_q * 1e3, 3), "Mkeys_s": round(n / t_q / 1e6, 1),
+                                     "GB_s": round(q_gbs, 1), "frac": round(q_gbs / peak, 4)},
+                           "clear": {"ms": round(t_clear * 1e3, 3),
+                                     "GB_s": round((1 << SP) * 8 / t_clear / 1e9, 1)}}}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline()
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 3), "unit": "Mkeys/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+                "data": "synthetic (seeded bijective keys, PCG64 values)",
+                "config": {"workload": "single map u32/u32: clear + insert 2^26 + retrieve 2^26 (50% hit)",
+                           "size_power": SP, "keys": n, "load_factor": 0.5, "parallelism": "replicas",
+                           "l2": "inputs larger than L2 (1 GiB table, 256 MiB arrays); no flush",
+                           "group_width": args.group or "default"},
+                "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+                "clocks": clocks}
+        print(json.dumps(line), flush=True)
+    m.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--group", type=int, default=0, help="probe-group width (0 = library default)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

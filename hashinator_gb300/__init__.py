@@ -1,0 +1,363 @@
+"""hashinator_gb300 — GB300-native Hashinator hot path.
+
+Python mirror of the reference's accelerated API over the C ABI of libhx.so
+(include/hx.h). Names follow Hashinator::Hashmap (hashinator/hashinator.h)
+and split::tools (splitvector/split_tools.h):
+
+    m = Hashmap(size_power=21, key_bytes=4)      # Hashmap<uint32_t,uint32_t>(21)
+    m.insert(keys, vals, target_lf=0.5)          # insert(keys, vals, len, targetLF)
+    m.retrieve(keys, out)                        # retrieve(keys, vals, len)
+    m.erase(keys)                                # erase(keys, len)
+    m.clean_tombstones()
+    n = m.extract_pattern(Pred.value_even(), out)
+    tools.copy_if(inp, out, Pred.mod_lt(100, 50))
+    tools.split_prefix_scan(inp, out)
+
+Arrays are CUDA tensors (torch) or raw device addresses (int). 4-byte keys
+use int32/uint32 tensors, 8-byte keys int64/uint64 tensors; values are
+reinterpreted bit-for-bit. The package never falls back to a CPU path: if
+libhx.so is missing, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+__all__ = ["lib", "HXError", "Hashmap", "Pred", "tools", "STATUS_SUCCESS", "STATUS_FAIL", "STATUS_INVALID",
+           "LIB_PATH", "Info"]
+
+LIB_PATH = Path(__file__).resolve().parent / "libhx.so"
+
+# hx_status
+HX_OK, HX_ERR_OVERFLOW, HX_ERR_OOM, HX_ERR_INVALID_ARG, HX_ERR_CUDA, HX_ERR_TIMEOUT, HX_ERR_CAPACITY = range(7)
+# Hashinator::status (common.h:85)
+STATUS_SUCCESS, STATUS_FAIL, STATUS_INVALID = 0, 1, 2
+
+PRED_ALL, PRED_MOD_LT, PRED_LT, PRED_GE, PRED_EQ, PRED_NE, PRED_MASK_EQ, PRED_RANGE, PRED_VALID, PRED_NOT_HOME = range(10)
+FIELD_ELEM, FIELD_KEY, FIELD_VALUE = 0, 1, 2
+PRED_SKIP_SENTINELS, PRED_NEGATE = 1, 2
+SCRATCH_SCAN, SCRATCH_COPY_IF = 0, 1
+
+
+class HXError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        msg = _lib_handle.hx_status_string(status).decode() if _lib_handle is not None else str(status)
+        extra = ""
+        if status == HX_ERR_CUDA and _lib_handle is not None:
+            extra = f" (cudaError {_lib_handle.hx_last_cuda_error()})"
+        super().__init__(f"{where}: {msg}{extra}")
+
+
+class Info(ctypes.Structure):
+    """hx_info, the host copy of Hashinator::Info (defaults.h:44-54)."""
+    _fields_ = [
+        ("size_power", ctypes.c_int32),
+        ("err", ctypes.c_int32),
+        ("fill", ctypes.c_uint64),
+        ("current_max_bucket_overflow", ctypes.c_uint64),
+        ("tombstone_counter", ctypes.c_uint64),
+        ("max_probe", ctypes.c_uint64),
+        ("bucket_count", ctypes.c_uint64),
+    ]
+
+
+class _CPred(ctypes.Structure):
+    _fields_ = [("op", ctypes.c_uint32), ("field", ctypes.c_uint32), ("flags", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("a", ctypes.c_uint64), ("b", ctypes.c_uint64)]
+
+
+_lib_handle = None
+
+_SIGS = {
+    "hx_map_create": [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
+    "hx_map_destroy": [ctypes.c_void_p],
+    "hx_insert": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_float, ctypes.c_void_p],
+    "hx_insert_pairs": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_float, ctypes.c_void_p],
+    "hx_retrieve": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p],
+    "hx_retrieve_pairs": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p],
+    "hx_erase": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p],
+    "hx_clean_tombstones": [ctypes.c_void_p, ctypes.c_void_p],
+    "hx_extract_pattern": [ctypes.c_void_p, ctypes.POINTER(_CPred), ctypes.c_void_p, ctypes.c_uint64,
+                           ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.c_void_p],
+    "hx_resize": [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p],
+    "hx_clear": [ctypes.c_void_p, ctypes.c_void_p],
+    "hx_get_info": [ctypes.c_void_p, ctypes.POINTER(Info), ctypes.c_void_p],
+    "hx_peek_status": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p],
+    "hx_bucket_data": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64)],
+    "hx_map_set_tuning": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int],
+    "hx_scratch_bytes": [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
+    "hx_exclusive_scan_u32": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
+                              ctypes.c_void_p],
+    "hx_copy_if": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(_CPred),
+                   ctypes.c_uint64, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.c_void_p,
+                   ctypes.c_uint64, ctypes.c_void_p],
+}
+_EXTRA_SIGS = {
+    "hx_status_string": ([ctypes.c_int], ctypes.c_char_p),
+    "hx_last_cuda_error": ([], ctypes.c_int),
+    "hx_kernel_launch_count": ([], ctypes.c_uint64),
+}
+
+
+def lib(path: str | os.PathLike | None = None) -> ctypes.CDLL:
+    """Load libhx.so (once). Raises if it has not been built."""
+    global _lib_handle
+    if _lib_handle is not None:
+        return _lib_handle
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with `python -m hashinator_gb300.build` "
+                           "(there is no CPU fallback)")
+    h = ctypes.CDLL(str(p))
+    for name, args in _SIGS.items():
+        f = getattr(h, name)
+        f.argtypes = args
+        f.restype = ctypes.c_int
+    for name, (args, res) in _EXTRA_SIGS.items():
+        f = getattr(h, name)
+        f.argtypes = args
+        f.restype = res
+    _lib_handle = h
+    for name, (args, res) in _OPTIONAL_SIGS.items():
+        f = getattr(h, name, None)
+        if f is not None:
+            f.argtypes = args
+            f.restype = res
+    return h
+
+
+_OPTIONAL_SIGS: dict = {}
+
+
+def _check(status: int, where: str) -> None:
+    if status != HX_OK:
+        raise HXError(status, where)
+
+
+def _ptr(x) -> int:
+    """Device address of a CUDA tensor or a raw int address."""
+    if x is None:
+        return 0
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        if not x.is_cuda:
+            raise ValueError("libhx takes device memory: pass a CUDA tensor")
+        if not x.is_contiguous():
+            raise ValueError("libhx takes contiguous arrays")
+        return x.data_ptr()
+    raise TypeError(f"cannot take a device address of {type(x)!r}")
+
+
+def _numel(x) -> int:
+    return x.numel() if hasattr(x, "numel") else len(x)
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        try:
+            import torch
+            return torch.cuda.current_stream().cuda_stream
+        except Exception:
+            return 0
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+class Pred:
+    """hx_pred descriptors for the reference's `Rule` functors."""
+
+    def __init__(self, op: int, field: int = FIELD_ELEM, a: int = 0, b: int = 0, flags: int = 0):
+        self.op, self.field, self.a, self.b, self.flags = op, field, a, b, flags
+
+    def c(self) -> _CPred:
+        return _CPred(self.op, self.field, self.flags, 0, self.a, self.b)
+
+    # scalar rules
+    @staticmethod
+    def mod_lt(a: int, s: int) -> "Pred":      # (x % a) < s
+        return Pred(PRED_MOD_LT, FIELD_ELEM, a, s)
+
+    @staticmethod
+    def even(field: int = FIELD_ELEM) -> "Pred":
+        return Pred(PRED_MASK_EQ, field, 1, 0)
+
+    @staticmethod
+    def lt(a: int, field: int = FIELD_ELEM) -> "Pred":
+        return Pred(PRED_LT, field, a)
+
+    # pair rules (extractPattern)
+    @staticmethod
+    def value_even(skip_sentinels: bool = True) -> "Pred":
+        return Pred(PRED_MASK_EQ, FIELD_VALUE, 1, 0, PRED_SKIP_SENTINELS if skip_sentinels else 0)
+
+    @staticmethod
+    def key_lt(a: int) -> "Pred":
+        return Pred(PRED_LT, FIELD_KEY, a)
+
+    @staticmethod
+    def valid_key() -> "Pred":
+        return Pred(PRED_VALID)
+
+    @staticmethod
+    def not_home() -> "Pred":
+        return Pred(PRED_NOT_HOME)
+
+
+class Hashmap:
+    """Hashinator::Hashmap<K,V> (hashinator.h:59-62) over libhx."""
+
+    def __init__(self, size_power: int = 5, key_bytes: int = 4, val_bytes: int | None = None, stream=None):
+        self._h = lib()
+        self._m = ctypes.c_void_p()
+        self.key_bytes = key_bytes
+        self.val_bytes = key_bytes if val_bytes is None else val_bytes
+        _check(self._h.hx_map_create(ctypes.byref(self._m), key_bytes, self.val_bytes, size_power,
+                                     _stream(stream)), "hx_map_create")
+
+    def close(self) -> None:
+        if self._m and self._m.value:
+            _check(self._h.hx_map_destroy(self._m), "hx_map_destroy")
+            self._m = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> int:
+        return self._m.value
+
+    # accelerated API -----------------------------------------------------
+    def insert(self, keys, vals, target_lf: float = 0.5, stream=None, n: int | None = None) -> None:
+        n = _numel(keys) if n is None else n
+        _check(self._h.hx_insert(self._m, _ptr(keys), _ptr(vals), n, target_lf, _stream(stream)), "hx_insert")
+
+    def insert_pairs(self, pairs, n: int | None = None, target_lf: float = 0.5, stream=None) -> None:
+        n = _numel(pairs) // 2 if n is None else n
+        _check(self._h.hx_insert_pairs(self._m, _ptr(pairs), n, target_lf, _stream(stream)), "hx_insert_pairs")
+
+    def retrieve(self, keys, vals, stream=None, n: int | None = None) -> None:
+        n = _numel(keys) if n is None else n
+        _check(self._h.hx_retrieve(self._m, _ptr(keys), _ptr(vals), n, _stream(stream)), "hx_retrieve")
+
+    def retrieve_pairs(self, pairs, n: int | None = None, stream=None) -> None:
+        n = _numel(pairs) // 2 if n is None else n
+        _check(self._h.hx_retrieve_pairs(self._m, _ptr(pairs), n, _stream(stream)), "hx_retrieve_pairs")
+
+    def erase(self, keys, stream=None, n: int | None = None) -> None:
+        n = _numel(keys) if n is None else n
+        _check(self._h.hx_erase(self._m, _ptr(keys), n, _stream(stream)), "hx_erase")
+
+    def clean_tombstones(self, stream=None) -> None:
+        _check(self._h.hx_clean_tombstones(self._m, _stream(stream)), "hx_clean_tombstones")
+
+    def extract_pattern(self, pred: Pred, out, capacity: int | None = None, stream=None, d_count=None) -> int:
+        """extractPattern(elements, rule): returns the count (synchronises)
+        unless d_count (a device address) is given, then returns -1."""
+        cap = (_numel(out) // 2) if capacity is None else capacity
+        cp = pred.c()
+        if d_count is not None:
+            _check(self._h.hx_extract_pattern(self._m, ctypes.byref(cp), _ptr(out), cap, _ptr(d_count), None,
+                                              _stream(stream)), "hx_extract_pattern")
+            return -1
+        cnt = ctypes.c_uint64()
+        st = self._h.hx_extract_pattern(self._m, ctypes.byref(cp), _ptr(out), cap, None, ctypes.byref(cnt),
+                                        _stream(stream))
+        if st not in (HX_OK, HX_ERR_CAPACITY):
+            _check(st, "hx_extract_pattern")
+        return cnt.value
+
+    def resize(self, new_size_power: int, stream=None) -> None:
+        _check(self._h.hx_resize(self._m, new_size_power, _stream(stream)), "hx_resize")
+
+    device_rehash = resize
+
+    def clear(self, stream=None) -> None:
+        _check(self._h.hx_clear(self._m, _stream(stream)), "hx_clear")
+
+    def set_tuning(self, group_width: int = 0, block_size: int = 0) -> None:
+        _check(self._h.hx_map_set_tuning(self._m, group_width, block_size), "hx_map_set_tuning")
+
+    # metadata (synchronous) ----------------------------------------------
+    def info(self, stream=None) -> Info:
+        inf = Info()
+        _check(self._h.hx_get_info(self._m, ctypes.byref(inf), _stream(stream)), "hx_get_info")
+        return inf
+
+    def size(self) -> int:
+        return self.info().fill
+
+    def bucket_count(self) -> int:
+        return self.info().bucket_count
+
+    def tombstone_count(self) -> int:
+        return self.info().tombstone_counter
+
+    def load_factor(self) -> float:
+        i = self.info()
+        return i.fill / i.bucket_count
+
+    def getSizePower(self) -> int:
+        return self.info().size_power
+
+    def peek_status(self, stream=None) -> int:
+        v = ctypes.c_int32()
+        _check(self._h.hx_peek_status(self._m, ctypes.byref(v), _stream(stream)), "hx_peek_status")
+        return v.value
+
+    def bucket_data(self) -> tuple[int, int]:
+        p = ctypes.c_void_p()
+        n = ctypes.c_uint64()
+        _check(self._h.hx_bucket_data(self._m, ctypes.byref(p), ctypes.byref(n)), "hx_bucket_data")
+        return p.value, n.value
+
+    def get_emptybucket(self) -> int:
+        return (1 << (8 * self.key_bytes)) - 1
+
+    def get_tombstone(self) -> int:
+        return (1 << (8 * self.key_bytes)) - 2
+
+
+class tools:
+    """split::tools (splitvector/split_tools.h)."""
+
+    @staticmethod
+    def scratch_bytes(op: int, n: int) -> int:
+        b = ctypes.c_uint64()
+        _check(lib().hx_scratch_bytes(op, n, ctypes.byref(b)), "hx_scratch_bytes")
+        return b.value
+
+    @staticmethod
+    def split_prefix_scan(inp, out, n: int | None = None, scratch=None, scratch_bytes: int = 0, stream=None) -> None:
+        n = _numel(inp) if n is None else n
+        _check(lib().hx_exclusive_scan_u32(_ptr(inp), _ptr(out), n, _ptr(scratch), scratch_bytes, _stream(stream)),
+               "hx_exclusive_scan_u32")
+
+    @staticmethod
+    def copy_if(inp, out, pred: Pred, elem_bytes: int = 4, n: int | None = None, capacity: int | None = None,
+                scratch=None, scratch_bytes: int = 0, stream=None, d_count=None) -> int:
+        if n is None:
+            n = _numel(inp) * inp.element_size() // elem_bytes
+        if capacity is None:
+            capacity = _numel(out) * out.element_size() // elem_bytes
+        cp = pred.c()
+        if d_count is not None:
+            _check(lib().hx_copy_if(_ptr(inp), _ptr(out), n, elem_bytes, ctypes.byref(cp), capacity, _ptr(d_count),
+                                    None, _ptr(scratch), scratch_bytes, _stream(stream)), "hx_copy_if")
+            return -1
+        cnt = ctypes.c_uint64()
+        st = lib().hx_copy_if(_ptr(inp), _ptr(out), n, elem_bytes, ctypes.byref(cp), capacity, None,
+                              ctypes.byref(cnt), _ptr(scratch), scratch_bytes, _stream(stream))
+        if st not in (HX_OK, HX_ERR_CAPACITY):
+            _check(st, "hx_copy_if")
+        return cnt.value
+
+
+def kernel_launch_count() -> int:
+    return lib().hx_kernel_launch_count()

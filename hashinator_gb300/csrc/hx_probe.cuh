@@ -1,0 +1,176 @@
+// hx_probe.cuh — probe-group linear probing over a power-of-two bucket array.
+//
+// The reference probes one key per 32-lane warp over a 32-bucket window that
+// starts at the key's home bucket (kernels_NVIDIA.h:356-408 insert, :665-689
+// erase, :753-773 retrieve): 256 B (u32) or 512 B (u64) read for the one or
+// two buckets a key needs at load factor 0.5. Here a probe group of G lanes
+// (G in {1,2,4,8,16,32}) serves one key, each lane reading B adjacent buckets
+// with one vector load, so a window is W = G*B buckets. Windows are aligned
+// to W buckets: the first window covers the home bucket's aligned block, and
+// lanes ignore the buckets before the home bucket in it. A 32-byte window is
+// exactly one DRAM sector.
+//
+// The probe order is the reference's linear order h, h+1, h+2, ... (mod 2^sp)
+// and the decisions per window are the reference's:
+//   insert:   key present in the window -> overwrite its value; else CAS the
+//             first EMPTY bucket in probe order; TOMBSTONE buckets are never
+//             reused; the whole table is the search bound.
+//   retrieve/ key present in the window -> hit; else an EMPTY bucket in the
+//   erase:    window -> miss; the bound is the longest probe of any key.
+// The distance of bucket b from home h is (b - h) mod 2^sp; max_probe holds
+// the largest distance + 1 ever placed (the reference keeps the same bound
+// rounded up to 32 in Info::currentMaxBucketOverflow, kernels_NVIDIA.h:436).
+#pragma once
+#include "hx_device.cuh"
+
+namespace hx {
+
+// Device-resident map metadata (the reference keeps Info in managed memory,
+// hashinator/defaults.h:44-54, and migrates it on every call).
+struct DInfo {
+  unsigned long long fill;
+  unsigned long long tombstones;
+  unsigned int max_probe;  // exact: largest (distance + 1); 0 for an empty map
+  int err;                 // HX_STATUS_*
+  unsigned long long moved;  // clean_tombstones: number of keys taken out
+  unsigned int skip;         // clean_tombstones: 1 when there were no tombstones
+  unsigned int pad;
+};
+
+enum : int { PR_CONTINUE = 0, PR_INSERTED = 1, PR_UPDATED = 2, PR_FAIL = 3 };
+
+template <int G>
+__device__ __forceinline__ unsigned group_mask(int lane) {
+  if constexpr (G == 32) return 0xffffffffu;
+  else return ((1u << G) - 1u) << (lane & ~(G - 1));
+}
+// Ballot over the G lanes of this group, as bits 0..G-1.
+template <int G>
+__device__ __forceinline__ unsigned group_ballot(unsigned gmask, int lane, bool p) {
+  if constexpr (G == 1) return p ? 1u : 0u;
+  else if constexpr (G == 32) return __ballot_sync(gmask, p);
+  else return (__ballot_sync(gmask, p) >> (lane & ~(G - 1))) & ((1u << G) - 1u);
+}
+template <int G, class T>
+__device__ __forceinline__ T group_shfl(unsigned gmask, T v, int src) {
+  if constexpr (G == 1) return v;
+  else return __shfl_sync(gmask, v, src, G);
+}
+
+// Insert or update one key. All G lanes of the group call it with the same
+// key. Returns PR_INSERTED / PR_UPDATED / PR_FAIL on every lane; `dist1`
+// receives distance + 1 on the lane that placed a new key, 0 elsewhere.
+template <class P, int G, int B>
+__device__ __forceinline__ int probe_insert(P* __restrict__ table, int sp, typename PairTraits<P>::K key,
+                                            typename PairTraits<P>::V val, int lane, unsigned gmask,
+                                            unsigned& dist1) {
+  using K = typename PairTraits<P>::K;
+  using V = typename PairTraits<P>::V;
+  constexpr K EMPTY = PairTraits<P>::EMPTY;
+  constexpr int W = G * B;
+  const int glane = lane & (G - 1);
+  const uint32_t tmask = (1u << sp) - 1u;
+  const long long tsize = (long long)tmask + 1;
+  const uint32_t h = home_slot(key, sp);
+  const uint32_t wstart = h & ~(uint32_t)(W - 1);
+  const int first = (int)(h - wstart);
+  for (uint32_t s = 0;; ++s) {
+    const long long d0 = (long long)s * W - first;  // distance of window offset 0
+    if (d0 >= tsize) return PR_FAIL;
+    P* wp = table + ((wstart + s * (uint32_t)W) & tmask) + glane * B;
+    K kk[B];
+    V vv[B];
+    load_buckets<B>(wp, kk, vv);
+    unsigned mbits = 0, ebits = 0;
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const long long d = d0 + glane * B + j;
+      const bool cons = d >= 0 && d < tsize;
+      if (cons && kk[j] == key) mbits |= 1u << j;
+      if (cons && kk[j] == EMPTY) ebits |= 1u << j;
+    }
+    const unsigned gm = group_ballot<G>(gmask, lane, mbits != 0);
+    if (gm) {
+      if (glane == __ffs(gm) - 1) store_value(wp + (__ffs(mbits) - 1), val);
+      return PR_UPDATED;
+    }
+    unsigned ge = group_ballot<G>(gmask, lane, ebits != 0);
+    while (ge) {
+      const int w = __ffs(ge) - 1;
+      int res = PR_CONTINUE;
+      if (glane == w) {
+        const int j = __ffs(ebits) - 1;
+        K ek = EMPTY;
+        V ev = vv[j];
+        for (int tries = 0;; ++tries) {
+          if (cas_pair(wp + j, ek, ev, key, val)) {
+            res = PR_INSERTED;
+            dist1 = (unsigned)(d0 + glane * B + j) + 1u;
+            break;
+          }
+          if (ek == key) {  // the same key won this bucket concurrently
+            store_value(wp + j, val);
+            res = PR_UPDATED;
+            break;
+          }
+          if (ek != EMPTY || tries >= 8) {
+            ebits &= ~(1u << j);
+            break;
+          }
+          // still EMPTY but with another stale value: retry with it
+        }
+      }
+      res = group_shfl<G>(gmask, res, w);
+      if (res != PR_CONTINUE) return res;
+      ge = group_ballot<G>(gmask, lane, ebits != 0);
+    }
+  }
+}
+
+// Find one key within `limit` buckets of its home. Returns the group lane
+// holding it (its bucket index in `slot`, value in `val`) or -1.
+template <class P, int G, int B>
+__device__ __forceinline__ int probe_find(const P* __restrict__ table, int sp, typename PairTraits<P>::K key,
+                                          unsigned limit, int lane, unsigned gmask, uint32_t& slot,
+                                          typename PairTraits<P>::V& val) {
+  using K = typename PairTraits<P>::K;
+  using V = typename PairTraits<P>::V;
+  constexpr K EMPTY = PairTraits<P>::EMPTY;
+  constexpr int W = G * B;
+  const int glane = lane & (G - 1);
+  const uint32_t tmask = (1u << sp) - 1u;
+  const uint32_t h = home_slot(key, sp);
+  const uint32_t wstart = h & ~(uint32_t)(W - 1);
+  const int first = (int)(h - wstart);
+  for (uint32_t s = 0;; ++s) {
+    const long long d0 = (long long)s * W - first;
+    if (d0 >= (long long)limit) return -1;
+    const uint32_t b0 = ((wstart + s * (uint32_t)W) & tmask) + glane * B;
+    K kk[B];
+    V vv[B];
+    load_buckets<B>(table + b0, kk, vv);
+    unsigned mbits = 0, ebits = 0;
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const long long d = d0 + glane * B + j;
+      const bool cons = d >= 0 && d < (long long)limit;
+      if (cons && kk[j] == key) mbits |= 1u << j;
+      if (cons && kk[j] == EMPTY) ebits |= 1u << j;
+    }
+    const unsigned gm = group_ballot<G>(gmask, lane, mbits != 0);
+    if (gm) {
+      const int w = __ffs(gm) - 1;
+      if (glane == w) {
+        const int j = __ffs(mbits) - 1;
+        slot = b0 + j;
+#pragma unroll
+        for (int t = 0; t < B; ++t)
+          if (t == j) val = vv[t];
+      }
+      return w;
+    }
+    if (group_ballot<G>(gmask, lane, ebits != 0)) return -1;
+  }
+}
+
+}  // namespace hx

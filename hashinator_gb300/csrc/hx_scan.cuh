@@ -1,0 +1,369 @@
+// hx_scan.cuh — single-pass scan and stable stream compaction.
+//
+// Replaces the reference's three-kernel compaction (scan_reduce_raw ->
+// split_prefix_scan_raw -> split_compact_raw, splitvector/split_tools.h:
+// 541-550, 556-602, 444-482) and its two-level Blelloch scan
+// (split_prescan + scan_add, split_tools.h:133-195, 78-88) with one pass over
+// the input: each CTA takes the next tile from an atomic ticket, reads it with
+// 128-bit loads, reduces it, publishes its aggregate, and resolves its
+// exclusive prefix by decoupled look-back over the tiles before it
+// (Merrill & Garland, "Single-pass Parallel Prefix Scan with Decoupled
+// Look-back", NVIDIA tech report NVR-2016-002). Input is read once and the
+// output written once: 8 B per element for the u32 scan, sizeof(T) * (n + c)
+// for compaction.
+//
+// Every wait on another tile's status is bounded: after kSpinLimit polls the
+// CTA records a timeout in the scratch error word and uses what it has; the
+// host turns that word into HX_ERR_TIMEOUT.
+#pragma once
+#include "hx_device.cuh"
+
+namespace hx {
+
+// Tile status word: bits 63..62 = flag, bits 61..0 = value.
+constexpr unsigned long long kStAgg = 1ull << 62;   // tile aggregate only
+constexpr unsigned long long kStInc = 2ull << 62;   // inclusive prefix
+constexpr unsigned long long kStVal = (1ull << 62) - 1;
+constexpr unsigned kSpinLimit = 1u << 22;
+
+// Scratch layout (hx_scratch_bytes): [ticket u32][error u32][pad .. 256 B]
+// [status u64 x tiles]. The host zeroes the first 256 + 8*tiles bytes before
+// each launch.
+struct ScanScratch {
+  unsigned int* ticket;
+  unsigned int* error;
+  unsigned long long* status;
+};
+
+__host__ __device__ inline uint64_t scan_scratch_bytes(uint64_t tiles) { return 256 + 8 * (tiles ? tiles : 1); }
+
+__device__ __forceinline__ unsigned long long ld_status(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_status(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned warp_incl_scan(unsigned x, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  return x;
+}
+
+// Look-back by warp 0 of the CTA: returns the exclusive prefix of `tile`
+// (sum of all earlier tiles, modulo 2^62 / 2^32 by caller) and publishes the
+// inclusive prefix. Called by all 32 lanes of warp 0.
+__device__ __forceinline__ unsigned long long lookback(const ScanScratch& sc, unsigned long long tile,
+                                                       unsigned long long aggregate, int lane) {
+  if (tile == 0) {
+    if (lane == 0) st_status(sc.status, kStInc | (aggregate & kStVal));
+    return 0;
+  }
+  if (lane == 0) st_status(sc.status + tile, kStAgg | (aggregate & kStVal));
+  unsigned long long exclusive = 0;
+  long long pred = (long long)tile - 1;
+  unsigned spins = 0;
+  bool timed_out = false;
+  while (true) {
+    const long long idx = pred - lane;
+    unsigned long long s = (idx >= 0) ? ld_status(sc.status + idx) : kStInc;  // before tile 0: prefix 0
+    // Wait until every lane in the window sees a published status.
+    while (__any_sync(0xffffffffu, (s >> 62) == 0)) {
+      if (++spins > kSpinLimit) {
+        timed_out = true;
+        break;
+      }
+      if (spins > 64) __nanosleep(spins > 4096 ? 256 : 32);
+      if ((s >> 62) == 0) s = ld_status(sc.status + idx);
+    }
+    if (timed_out) {
+      if (lane == 0) atomicExch(sc.error, 1u);
+      break;
+    }
+    const unsigned inc_mask = __ballot_sync(0xffffffffu, (s >> 62) == 2);
+    // Lanes up to and including the closest inclusive prefix contribute.
+    const int stop = inc_mask ? (__ffs(inc_mask) - 1) : 31;
+    unsigned long long v = (lane <= stop && idx >= 0) ? (s & kStVal) : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    exclusive += v;
+    if (inc_mask) break;
+    pred -= 32;
+  }
+  if (lane == 0) st_status(sc.status + tile, kStInc | ((exclusive + aggregate) & kStVal));
+  return exclusive;
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive u32 sum scan. CTA = BLOCK threads; each warp owns a contiguous
+// chunk of 32*R uint4 (128*R elements); the tile is BLOCK/32 chunks.
+// Thread (warp w, lane l) holds uint4 number r*32+l of its chunk, r < R, so
+// every load and store instruction of the warp covers 512 contiguous bytes.
+// ---------------------------------------------------------------------------
+template <int BLOCK, int R>
+__global__ void __launch_bounds__(BLOCK) k_scan_u32(const uint32_t* in, uint32_t* out,
+                                                   uint64_t n, ScanScratch sc, bool vec) {
+  constexpr int WARPS = BLOCK / 32;
+  constexpr uint64_t TILE = (uint64_t)BLOCK * R * 4;
+  __shared__ unsigned s_warp[WARPS];
+  __shared__ unsigned long long s_tile;
+  __shared__ unsigned s_prefix;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_tile = atomicAdd(sc.ticket, 1u);
+  __syncthreads();
+  const unsigned long long tile = s_tile;
+  const uint64_t chunk = tile * TILE + (uint64_t)warp * 32 * R * 4;
+
+  uint32_t x[R][4];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const uint64_t e = chunk + ((uint64_t)r * 32 + lane) * 4;
+    if (vec && e + 4 <= n) {
+      uint4 q = __ldcs(reinterpret_cast<const uint4*>(in + e));
+      x[r][0] = q.x; x[r][1] = q.y; x[r][2] = q.z; x[r][3] = q.w;
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) x[r][q] = (e + q < n) ? in[e + q] : 0u;
+    }
+  }
+  // Warp-level exclusive prefixes of each held uint4.
+  unsigned pre[R];
+  unsigned acc = 0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const unsigned s = x[r][0] + x[r][1] + x[r][2] + x[r][3];
+    const unsigned incl = warp_incl_scan(s, lane);
+    pre[r] = acc + incl - s;
+    acc += __shfl_sync(0xffffffffu, incl, 31);
+  }
+  if (lane == 0) s_warp[warp] = acc;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned wt = (lane < WARPS) ? s_warp[lane] : 0u;
+    const unsigned wincl = warp_incl_scan(wt, lane);
+    const unsigned aggregate = __shfl_sync(0xffffffffu, wincl, 31);
+    const unsigned long long tp = lookback(sc, tile, aggregate, lane);
+    if (lane < WARPS) s_warp[lane] = wincl - wt;  // exclusive warp offsets
+    if (lane == 0) s_prefix = (unsigned)tp;
+  }
+  __syncthreads();
+  const unsigned base = s_prefix + s_warp[warp];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const uint64_t e = chunk + ((uint64_t)r * 32 + lane) * 4;
+    unsigned o0 = base + pre[r];
+    unsigned o1 = o0 + x[r][0];
+    unsigned o2 = o1 + x[r][1];
+    unsigned o3 = o2 + x[r][2];
+    if (vec && e + 4 <= n) {
+      __stcs(reinterpret_cast<uint4*>(out + e), make_uint4(o0, o1, o2, o3));
+    } else {
+      const unsigned o[4] = {o0, o1, o2, o3};
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (e + q < n) out[e + q] = o[q];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stable compaction of T (uint32_t, P32 or P64): E = 16/sizeof(T) elements
+// per uint4. Selected elements are staged in shared memory in output order
+// and written out as one contiguous run per tile with coalesced stores.
+// The count of the last tile's inclusive prefix goes to *d_count.
+// ---------------------------------------------------------------------------
+template <class T>
+struct ElemOps;
+template <>
+struct ElemOps<uint32_t> {
+  static constexpr int E = 4;
+  struct Ctx {};
+  __device__ static bool pred(const hx_pred& p, const uint32_t& x, const Ctx&) {
+    bool r = pred_on32(p, x);
+    return (p.flags & HX_PRED_NEGATE) ? !r : r;
+  }
+};
+template <>
+struct ElemOps<P32> {
+  static constexpr int E = 2;
+  using Ctx = TableRef<P32>;
+  __device__ static bool pred(const hx_pred& p, const P32& x, const Ctx& c) {
+    return pred_pair<P32>(p, x.first, x.second, c);
+  }
+};
+template <>
+struct ElemOps<P64> {
+  static constexpr int E = 1;
+  using Ctx = TableRef<P64>;
+  __device__ static bool pred(const hx_pred& p, const P64& x, const Ctx& c) {
+    return pred_pair<P64>(p, x.first, x.second, c);
+  }
+};
+
+template <class T>
+__device__ __forceinline__ void load_vec(const T* p, T (&v)[16 / sizeof(T)]) {
+  uint4 q = __ldcs(reinterpret_cast<const uint4*>(p));
+  memcpy(&v[0], &q, 16);
+}
+
+// clean_tombstones mode (CLEAN): the input is the bucket array itself. Every
+// TOMBSTONE bucket and every selected (moved) bucket is rewritten to
+// (EMPTY, 0) after it has been read, the last tile takes the moved count off
+// fill, and the whole pass is skipped when *skip is set. Reading a home
+// bucket that another CTA rewrites at the same time cannot change a decision:
+// a key Y is "not home" iff bucket[home(Y)] holds a key other than Y, and that
+// bucket only ever changes between keys other than Y and EMPTY.
+struct CleanArgs {
+  const unsigned* skip;
+  unsigned long long* fill;
+};
+
+template <class T, int BLOCK, int R, bool CLEAN>
+__global__ void __launch_bounds__(BLOCK) k_compact(const T* __restrict__ in, T* __restrict__ out, uint64_t n,
+                                                  hx_pred pr, typename ElemOps<T>::Ctx ctx, uint64_t capacity,
+                                                  unsigned long long* d_count, ScanScratch sc, bool vec,
+                                                  CleanArgs cl) {
+  constexpr int E = ElemOps<T>::E;
+  constexpr int WARPS = BLOCK / 32;
+  constexpr uint64_t TILE = (uint64_t)BLOCK * R * E;
+  __shared__ unsigned s_warp[WARPS];
+  __shared__ unsigned long long s_tile, s_prefix;
+  __shared__ unsigned s_total;
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  T* s_out = reinterpret_cast<T*>(s_raw);
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if constexpr (CLEAN) {
+    if (*cl.skip) return;
+  }
+  if (threadIdx.x == 0) s_tile = atomicAdd(sc.ticket, 1u);
+  __syncthreads();
+  const unsigned long long tile = s_tile;
+  const uint64_t tile0 = tile * TILE;
+  const uint64_t chunk = tile0 + (uint64_t)warp * 32 * R * E;
+
+  T x[R][E];
+  unsigned f[R];  // selection bits of each held uint4
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const uint64_t e = chunk + ((uint64_t)r * 32 + lane) * E;
+    if (vec && e + E <= n) {
+      load_vec<T>(in + e, x[r]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < E; ++q)
+        if (e + q < n) x[r][q] = in[e + q];
+    }
+    unsigned bits = 0;
+#pragma unroll
+    for (int q = 0; q < E; ++q)
+      if (e + q < n && ElemOps<T>::pred(pr, x[r][q], ctx)) bits |= 1u << q;
+    f[r] = bits;
+    if constexpr (CLEAN) {
+      using Tr = PairTraits<T>;
+#pragma unroll
+      for (int q = 0; q < E; ++q)
+        if (e + q < n && ((bits >> q) & 1u || x[r][q].first == Tr::TOMB)) {
+          T empty;
+          empty.first = Tr::EMPTY;
+          empty.second = 0;
+          const_cast<T*>(in)[e + q] = empty;
+        }
+    }
+  }
+  unsigned pre[R];
+  unsigned acc = 0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const unsigned c = __popc(f[r]);
+    const unsigned incl = warp_incl_scan(c, lane);
+    pre[r] = acc + incl - c;
+    acc += __shfl_sync(0xffffffffu, incl, 31);
+  }
+  if (lane == 0) s_warp[warp] = acc;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned wt = (lane < WARPS) ? s_warp[lane] : 0u;
+    const unsigned wincl = warp_incl_scan(wt, lane);
+    const unsigned aggregate = __shfl_sync(0xffffffffu, wincl, 31);
+    const unsigned long long tp = lookback(sc, tile, aggregate, lane);
+    if (lane < WARPS) s_warp[lane] = wincl - wt;
+    if (lane == 0) {
+      s_prefix = tp;
+      s_total = aggregate;
+      if (tile0 + TILE >= n) {  // last tile
+        if (d_count) *d_count = tp + aggregate;
+        if constexpr (CLEAN) atomicAdd(cl.fill, 0ull - (tp + aggregate));
+      }
+    }
+  }
+  __syncthreads();
+  // Stage selected elements at their tile-local output index.
+  const unsigned wbase = s_warp[warp];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    unsigned o = wbase + pre[r];
+#pragma unroll
+    for (int q = 0; q < E; ++q)
+      if (f[r] & (1u << q)) s_out[o++] = x[r][q];
+  }
+  __syncthreads();
+  const unsigned total = s_total;
+  const unsigned long long prefix = s_prefix;
+  for (unsigned i = threadIdx.x; i < total; i += BLOCK) {
+    const unsigned long long dst = prefix + i;
+    if (dst < capacity) out[dst] = s_out[i];
+  }
+}
+
+// ---- host launch helpers ---------------------------------------------------
+constexpr int kScanBlock = 256;
+constexpr int kScanR = 4;  // 256 threads x 4 uint4 = 4096 u32 per tile
+constexpr int kCompactBlock = 256;
+constexpr int kCompactR = 4;  // 256 threads x 4 uint4 = 16 KiB per tile
+
+inline uint64_t scan_tiles(uint64_t n) {
+  const uint64_t t = (uint64_t)kScanBlock * kScanR * 4;
+  return (n + t - 1) / t;
+}
+template <class T>
+inline uint64_t compact_tile_elems() {
+  return (uint64_t)kCompactBlock * kCompactR * (16 / sizeof(T));
+}
+template <class T>
+inline uint64_t compact_tiles(uint64_t n) {
+  const uint64_t t = compact_tile_elems<T>();
+  return (n + t - 1) / t;
+}
+inline ScanScratch carve_scratch(void* p, uint64_t tiles) {
+  ScanScratch sc;
+  sc.ticket = reinterpret_cast<unsigned int*>(p);
+  sc.error = sc.ticket + 1;
+  sc.status = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(p) + 256);
+  (void)tiles;
+  return sc;
+}
+
+// Launch one compaction pass (n > 0). The scratch must hold
+// scan_scratch_bytes(compact_tiles<T>(n)) bytes; it is zeroed here.
+template <class T, bool CLEAN>
+inline cudaError_t launch_compact(const T* in, T* out, uint64_t n, const hx_pred& pr,
+                                  typename ElemOps<T>::Ctx ctx, uint64_t capacity, unsigned long long* d_count,
+                                  void* scratch, CleanArgs cl, cudaStream_t s) {
+  const uint64_t tiles = compact_tiles<T>(n);
+  cudaError_t e = cudaMemsetAsync(scratch, 0, scan_scratch_bytes(tiles), s);
+  if (e != cudaSuccess) return e;
+  const bool vec = ((uintptr_t)in % 16) == 0;
+  const size_t smem = (size_t)compact_tile_elems<T>() * sizeof(T);
+  auto kern = k_compact<T, kCompactBlock, kCompactR, CLEAN>;
+  kern<<<(unsigned)tiles, kCompactBlock, smem, s>>>(in, out, n, pr, ctx, capacity, d_count,
+                                                   carve_scratch(scratch, tiles), vec, cl);
+  return cudaGetLastError();
+}
+
+}  // namespace hx

@@ -1,0 +1,221 @@
+/*
+ * hx.h — C ABI of the GB300-native Hashinator hot path (libhx.so).
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes and
+ * returns an hx_status. Device pointers must be device-accessible memory
+ * (cudaMalloc, cudaMallocAsync or managed). Streams are passed as opaque
+ * `hx_stream` values (a cudaStream_t; NULL = the legacy default stream).
+ *
+ * Calls are stream-ordered and asynchronous unless their comment says they
+ * synchronise. The reference blocks the host after every kernel
+ * (hashinator/hashers.h:55,76,98,118,128,140,151,161); a caller that wants
+ * that behaviour calls cudaStreamSynchronize, or hx_get_info, afterwards.
+ *
+ * Each declaration names the reference interface it replaces
+ * (path:line inside the Hashinator source tree, version 1.0.1).
+ */
+#ifndef HX_H
+#define HX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void* hx_stream; /* cudaStream_t */
+
+/* Return codes. The reference aborts on CUDA errors (SPLIT_CHECK_ERR,
+ * splitvector/split_allocators.h:33-40) and reports a full table through
+ * Info::err = status::fail (hashinator/kernels_NVIDIA.h:443-445). */
+typedef enum hx_status {
+  HX_OK = 0,
+  HX_ERR_OVERFLOW = 1,    /* insert could not place every key: table full      */
+  HX_ERR_OOM = 2,         /* device allocation failed                          */
+  HX_ERR_INVALID_ARG = 3, /* bad pointer, size, type or size power             */
+  HX_ERR_CUDA = 4,        /* a CUDA runtime call failed (see hx_last_cuda_error)*/
+  HX_ERR_TIMEOUT = 5,     /* a bounded device-side wait ran out                */
+  HX_ERR_CAPACITY = 6     /* the output buffer is smaller than the result      */
+} hx_status;
+
+/* Hashinator::status (common.h:85): values of hx_info.err. */
+enum { HX_STATUS_SUCCESS = 0, HX_STATUS_FAIL = 1, HX_STATUS_INVALID = 2 };
+
+/* Host copy of the map metadata, mirroring Hashinator::Info
+ * (hashinator/defaults.h:44-54). current_max_bucket_overflow keeps the
+ * reference's meaning (the probe bound rounded up to a multiple of 32,
+ * never below 32, common.h:54-57); max_probe is the exact longest probe
+ * (distance + 1) that the device kernels use as their search bound. */
+typedef struct hx_info {
+  int32_t size_power;
+  int32_t err;
+  uint64_t fill;
+  uint64_t current_max_bucket_overflow;
+  uint64_t tombstone_counter;
+  uint64_t max_probe;
+  uint64_t bucket_count;
+} hx_info;
+
+/* Predicate descriptor: the C-ABI stand-in for the reference's `Rule`
+ * functors (split_tools.h:1129, hashinator.h:1155). A user functor cannot
+ * cross a C ABI; the descriptor covers the rules the reference's own tests,
+ * benchmarks and clean_tombstones use. Evaluated on one field x:
+ *   HX_PRED_ALL      true
+ *   HX_PRED_MOD_LT   (x % a) <  b            (a != 0)
+ *   HX_PRED_LT       x <  a
+ *   HX_PRED_GE       x >= a
+ *   HX_PRED_EQ       x == a
+ *   HX_PRED_NE       x != a
+ *   HX_PRED_MASK_EQ  (x & a) == b            (even: a=1,b=0; odd: a=1,b=1)
+ *   HX_PRED_RANGE    a <= x < b
+ *   HX_PRED_VALID    key is neither EMPTY nor TOMBSTONE (field ignored)
+ *   HX_PRED_NOT_HOME valid key that does not sit in its home bucket
+ *                    (map extraction only; the clean_tombstones rule,
+ *                    hashinator.h:1285-1297, without its side effect)
+ * field: HX_FIELD_ELEM for scalar arrays, HX_FIELD_KEY / HX_FIELD_VALUE for
+ * hash_pair arrays. flags: HX_PRED_SKIP_SENTINELS makes a pair predicate
+ * false on EMPTY and TOMBSTONE buckets (the reference's rules see those
+ * buckets too, so the default keeps them); HX_PRED_NEGATE inverts. */
+enum {
+  HX_PRED_ALL = 0,
+  HX_PRED_MOD_LT = 1,
+  HX_PRED_LT = 2,
+  HX_PRED_GE = 3,
+  HX_PRED_EQ = 4,
+  HX_PRED_NE = 5,
+  HX_PRED_MASK_EQ = 6,
+  HX_PRED_RANGE = 7,
+  HX_PRED_VALID = 8,
+  HX_PRED_NOT_HOME = 9
+};
+enum { HX_FIELD_ELEM = 0, HX_FIELD_KEY = 1, HX_FIELD_VALUE = 2 };
+enum { HX_PRED_SKIP_SENTINELS = 1u, HX_PRED_NEGATE = 2u };
+
+typedef struct hx_pred {
+  uint32_t op;
+  uint32_t field;
+  uint32_t flags;
+  uint32_t reserved;
+  uint64_t a;
+  uint64_t b;
+} hx_pred;
+
+typedef struct hx_map hx_map;
+
+/* ---- map lifetime ------------------------------------------------------ */
+
+/* Hashmap(int sizepower) (hashinator.h:120-129): a table of 2^size_power
+ * buckets, every bucket (EMPTY, 0). key_bytes/val_bytes in {4, 8}:
+ * (4,4) and (8,8) are hash_pair<uint32_t,uint32_t> (8 B) and
+ * hash_pair<uint64_t,uint64_t> (16 B). EMPTY = all ones, TOMBSTONE =
+ * EMPTY - 1 (hashinator.h:59-60). 1 <= size_power <= 31. Synchronises. */
+hx_status hx_map_create(hx_map** out, int key_bytes, int val_bytes, int size_power, hx_stream stream);
+
+/* ~Hashmap() (hashinator.h:213-216). Synchronises the device. */
+hx_status hx_map_destroy(hx_map* map);
+
+/* ---- the accelerated API (hashinator.h:1262-1409) ----------------------- */
+
+/* insert(KEY*, VAL*, size_t, float targetLF = 0.5, stream) (hashinator.h:1319-1335).
+ * Upsert of n keys. Grows the table first, like the reference, when
+ * ceil(log2((fill + n) / target_lf)) exceeds the size power (target_lf <= 0
+ * disables growth). Sets err = success, or fail if a key found no bucket. */
+hx_status hx_insert(hx_map* map, const void* d_keys, const void* d_vals, uint64_t n, float target_lf,
+                    hx_stream stream);
+
+/* insert(hash_pair*, size_t, float targetLF = 0.5, stream) (hashinator.h:1359-1374). */
+hx_status hx_insert_pairs(hx_map* map, const void* d_pairs, uint64_t n, float target_lf, hx_stream stream);
+
+/* retrieve(KEY*, VAL*, size_t, stream) (hashinator.h:1378-1384): d_vals[i]
+ * receives the value of d_keys[i]; a missing key leaves d_vals[i] as it was. */
+hx_status hx_retrieve(hx_map* map, const void* d_keys, void* d_vals, uint64_t n, hx_stream stream);
+
+/* retrieve(hash_pair*, size_t, stream) (hashinator.h:1388-1394): writes
+ * pairs[i].second for every key found. */
+hx_status hx_retrieve_pairs(hx_map* map, void* d_pairs, uint64_t n, hx_stream stream);
+
+/* erase(KEY*, size_t, stream) (hashinator.h:1398-1409): present keys become
+ * TOMBSTONE; fill drops and tombstone_counter grows by the number erased. */
+hx_status hx_erase(hx_map* map, const void* d_keys, uint64_t n, hx_stream stream);
+
+/* clean_tombstones(stream) (hashinator.h:1262-1315): every TOMBSTONE bucket
+ * becomes EMPTY and every key that does not sit in its home bucket is taken
+ * out and inserted again; fill is unchanged, tombstone_counter becomes 0.
+ * Uses a map-owned device buffer (grown on demand) for the moved keys. */
+hx_status hx_clean_tombstones(hx_map* map, hx_stream stream);
+
+/* extractPattern(hash_pair*, Rule, stream) (hashinator.h:1168-1185) and
+ * extractPattern(SplitVector&, Rule, stream) (:1155-1165): order-preserving
+ * copy of the buckets for which pred holds, in bucket order. At most
+ * `capacity` pairs are written. The count goes to *d_count (device memory,
+ * stream-ordered) if d_count is not NULL, and to *h_count (host memory,
+ * the call then synchronises) if h_count is not NULL. A synchronous call
+ * returns HX_ERR_CAPACITY when the count exceeds capacity. */
+hx_status hx_extract_pattern(hx_map* map, const hx_pred* pred, void* d_out, uint64_t capacity, uint64_t* d_count,
+                             uint64_t* h_count, hx_stream stream);
+
+/* resize(newSizePower, targets::device, stream) = device_rehash
+ * (hashinator.h:285-336, :552-566): every valid pair moves into a new table
+ * of 2^new_size_power buckets in one streaming pass; tombstones are dropped.
+ * Sets err = success if fill is preserved. */
+hx_status hx_resize(hx_map* map, int new_size_power, hx_stream stream);
+
+/* clear(targets::device, stream) (hashinator.h:492-518): every bucket
+ * becomes (EMPTY, 0); fill, tombstones and the probe bound go to zero. */
+hx_status hx_clear(hx_map* map, hx_stream stream);
+
+/* size(), bucket_count(), tombstone_count(), load_factor(), getSizePower(),
+ * copyMetadata(Info*, stream) (hashinator.h:441-457, 611, 228-230).
+ * Synchronises the stream. */
+hx_status hx_get_info(hx_map* map, hx_info* out, hx_stream stream);
+
+/* peek_status() (hashinator.h:434-438): returns err and resets it to
+ * invalid. Synchronises the stream. */
+hx_status hx_peek_status(hx_map* map, int32_t* out, hx_stream stream);
+
+/* expose_bucketdata() (hashinator.h:477-483): the device bucket array. */
+hx_status hx_bucket_data(hx_map* map, void** d_buckets, uint64_t* bucket_count);
+
+/* Probe-group tuning (no reference counterpart: the reference fixes one
+ * 32-lane warp per key, hashinator/defaults.h:26-38). group_width in
+ * {1,2,4,8,16,32} lanes per key; block_size a multiple of 32 up to 1024;
+ * 0 keeps the current value. */
+hx_status hx_map_set_tuning(hx_map* map, int group_width, int block_size);
+
+/* ---- split::tools (splitvector/split_tools.h) -------------------------- */
+
+/* Device scratch bytes that hx_exclusive_scan_u32 (op 0) or hx_copy_if
+ * (op 1) needs for n elements; the replacement of
+ * estimateMemoryForCompaction (split_tools.h:1065-1090). */
+enum { HX_SCRATCH_SCAN = 0, HX_SCRATCH_COPY_IF = 1 };
+hx_status hx_scratch_bytes(int op, uint64_t n, uint64_t* bytes);
+
+/* split_prefix_scan(in, out, stream) (split_tools.h:363-418) for uint32:
+ * exclusive sum, wrapping modulo 2^32, any n (the reference asserts a power
+ * of two). d_scratch may be NULL (then it is allocated stream-ordered) or a
+ * caller buffer of hx_scratch_bytes(HX_SCRATCH_SCAN, n) bytes. In-place
+ * (d_out == d_in) is allowed. */
+hx_status hx_exclusive_scan_u32(const uint32_t* d_in, uint32_t* d_out, uint64_t n, void* d_scratch,
+                                uint64_t scratch_bytes, hx_stream stream);
+
+/* copy_if(in, out, Rule, stream) (split_tools.h:1129-1223): stable stream
+ * compaction of n elements of elem_bytes in {4, 8, 16} (uint32_t,
+ * hash_pair<u32,u32>, hash_pair<u64,u64>). Count reporting and capacity
+ * as for hx_extract_pattern. */
+hx_status hx_copy_if(const void* d_in, void* d_out, uint64_t n, int elem_bytes, const hx_pred* pred,
+                     uint64_t capacity, uint64_t* d_count, uint64_t* h_count, void* d_scratch,
+                     uint64_t scratch_bytes, hx_stream stream);
+
+/* ---- diagnostics -------------------------------------------------------- */
+
+const char* hx_status_string(hx_status status);
+/* The last cudaError_t value seen by the library on this host thread. */
+int hx_last_cuda_error(void);
+/* Number of kernels libhx has launched in this process. */
+uint64_t hx_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HX_H */

@@ -1,0 +1,55 @@
+"""CPU checks of the C-ABI boundary: libhx.so builds, loads, and exports every
+entry point declared in include/*.h (no compute calls: no GPU here)."""
+import ctypes
+import re
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    syms = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(hx_[a-z0-9_]+)\s*\(", text, flags=re.M):
+            syms.add(m.group(1))
+    return sorted(syms)
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for must in ("hx_map_create", "hx_insert", "hx_insert_pairs", "hx_retrieve", "hx_retrieve_pairs", "hx_erase",
+                 "hx_clean_tombstones", "hx_extract_pattern", "hx_copy_if", "hx_exclusive_scan_u32"):
+        assert must in syms
+
+
+def test_library_exports_every_declared_symbol(hx):
+    lib = ctypes.CDLL(str(hx.LIB_PATH))
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_status_strings_and_argument_checks(hx):
+    lib = hx.lib()
+    assert lib.hx_status_string(0) == b"ok"
+    # argument validation happens before any device work
+    out = ctypes.c_void_p()
+    assert lib.hx_map_create(ctypes.byref(out), 4, 8, 10, None) == hx.HX_ERR_INVALID_ARG
+    assert lib.hx_map_create(ctypes.byref(out), 4, 4, 0, None) == hx.HX_ERR_INVALID_ARG
+    assert lib.hx_map_create(ctypes.byref(out), 4, 4, 32, None) == hx.HX_ERR_INVALID_ARG
+    assert lib.hx_insert(None, None, None, 0, 0.5, None) == hx.HX_ERR_INVALID_ARG
+    assert lib.hx_retrieve(None, None, None, 0, None) == hx.HX_ERR_INVALID_ARG
+    b = ctypes.c_uint64()
+    assert lib.hx_scratch_bytes(7, 10, ctypes.byref(b)) == hx.HX_ERR_INVALID_ARG
+    assert lib.hx_scratch_bytes(hx.SCRATCH_SCAN, 1 << 20, ctypes.byref(b)) == hx.HX_OK and b.value > 256
+    p = hx.Pred.mod_lt(0, 1).c()
+    assert lib.hx_copy_if(None, None, 0, 4, ctypes.byref(p), 0, None, None, None, 0, None) == hx.HX_ERR_INVALID_ARG
+    assert lib.hx_exclusive_scan_u32(None, None, 0, None, 0, None) == hx.HX_OK  # n == 0 is a no-op
+
+
+def test_no_cpu_fallback_in_product():
+    """The product package must not reach into the oracle."""
+    for p in (ROOT / "hashinator_gb300").rglob("*.py"):
+        src = p.read_text()
+        assert "import oracle" not in src and "from oracle" not in src, p

@@ -1,0 +1,124 @@
+"""GPU parity of split::tools replacements (copy_if, split_prefix_scan)
+against the oracle, plus the reference's own known answers (race.cu,
+unit.cu)."""
+import numpy as np
+import pytest
+
+from gpu_util import from_dev, to_dev
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [1, 2, 3, 31, 32, 33, 100, 1023, 1024, 1025, 2999, 4095, 4096, 4097, 65535, 65536, 1 << 20,
+         (1 << 20) + 17, 3_000_001]
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_scan_matches_oracle(hx, oracle_mod, n):
+    x = np.random.default_rng(n).integers(0, 16, size=n, dtype=np.uint32)
+    out = to_dev(np.zeros(n, np.uint32))
+    hx.tools.split_prefix_scan(to_dev(x), out)
+    np.testing.assert_array_equal(from_dev(out, np.uint32), oracle_mod.exclusive_scan_u32(x))
+
+
+@pytest.mark.parametrize("power", range(2, 18))
+def test_scan_iota_known_answer(hx, power):
+    # race.cu: input[i] = i, exclusive scan == thrust::exclusive_scan (wraps mod 2^32)
+    n = 1 << power
+    out = to_dev(np.zeros(n, np.uint32))
+    hx.tools.split_prefix_scan(to_dev(np.arange(n, dtype=np.uint32)), out)
+    i = np.arange(n, dtype=np.uint64)
+    np.testing.assert_array_equal(from_dev(out, np.uint32), ((i * (i - 1)) // 2 % (1 << 32)).astype(np.uint32))
+
+
+def test_scan_wraps_and_in_place(hx, oracle_mod):
+    x = np.full(1 << 20, 0xFFFFFFF0, np.uint32)
+    d = to_dev(x)
+    hx.tools.split_prefix_scan(d, d)  # in place
+    np.testing.assert_array_equal(from_dev(d, np.uint32), oracle_mod.exclusive_scan_u32(x))
+
+
+def test_scan_caller_scratch(hx, oracle_mod):
+    import torch
+    n = 1_000_003
+    x = np.random.default_rng(1).integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
+    nb = hx.tools.scratch_bytes(hx.SCRATCH_SCAN, n)
+    scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    out = to_dev(np.zeros(n, np.uint32))
+    for _ in range(2):
+        hx.tools.split_prefix_scan(to_dev(x), out, scratch=scratch, scratch_bytes=nb)
+        np.testing.assert_array_equal(from_dev(out, np.uint32), oracle_mod.exclusive_scan_u32(x))
+    with pytest.raises(hx.HXError):
+        hx.tools.split_prefix_scan(to_dev(x), out, scratch=scratch, scratch_bytes=16)
+
+
+@pytest.mark.parametrize("n", SIZES)
+@pytest.mark.parametrize("s", [1, 50, 99])
+def test_copy_if_u32_mod_lt(hx, oracle_mod, n, s):
+    x = np.random.default_rng(n + s).integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
+    out = to_dev(np.zeros(n, np.uint32))
+    c = hx.tools.copy_if(to_dev(x), out, hx.Pred.mod_lt(100, s))
+    want = oracle_mod.copy_if(x, 4, oracle_mod.pred(1, 0, 100, s))
+    assert c == len(want)
+    np.testing.assert_array_equal(from_dev(out, np.uint32)[:c], want)
+
+
+@pytest.mark.parametrize("power", range(5, 25, 3))
+def test_copy_if_iota_evens(hx, power):
+    n = 1 << power
+    out = to_dev(np.zeros(n, np.uint32))
+    c = hx.tools.copy_if(to_dev(np.arange(n, dtype=np.uint32)), out, hx.Pred.even())
+    assert c == n // 2
+    np.testing.assert_array_equal(from_dev(out, np.uint32)[:c], np.arange(0, n, 2, dtype=np.uint32))
+
+
+@pytest.mark.parametrize("size", list(range(32, 3000, 97)) + [2999])
+def test_copy_if_flag_split(hx, size):
+    # unit.cu Compaction_Tests_Linear: 8-byte {num, flag} elements, both splits
+    num = np.arange(1, size + 1, dtype=np.uint32)
+    arr = np.stack([num, (num % 2 == 0).astype(np.uint32)], axis=1).reshape(-1)
+    d = to_dev(arr)
+    on, off = to_dev(np.zeros_like(arr)), to_dev(np.zeros_like(arr))
+    c1 = hx.tools.copy_if(d, on, hx.Pred(hx.PRED_EQ, hx.FIELD_VALUE, 1), elem_bytes=8)
+    c0 = hx.tools.copy_if(d, off, hx.Pred(hx.PRED_EQ, hx.FIELD_VALUE, 0), elem_bytes=8)
+    assert c1 + c0 == size and c1 == size // 2
+    a1 = from_dev(on, np.uint32).reshape(-1, 2)[:c1]
+    a0 = from_dev(off, np.uint32).reshape(-1, 2)[:c0]
+    assert (a1[:, 1] == 1).all() and (a0[:, 1] == 0).all()
+    np.testing.assert_array_equal(a1[:, 0], num[num % 2 == 0])
+
+
+@pytest.mark.parametrize("eb", [8, 16])
+@pytest.mark.parametrize("n", [5, 1000, 123457])
+def test_copy_if_pairs_matches_oracle(hx, oracle_mod, eb, n):
+    dt = np.uint32 if eb == 8 else np.uint64
+    rng = np.random.default_rng(eb * n)
+    arr = rng.integers(0, np.iinfo(dt).max, size=2 * n, dtype=dt, endpoint=True)
+    arr[::7] = np.iinfo(dt).max  # EMPTY keys in the mix
+    out = to_dev(np.zeros_like(arr))
+    for hp, op in [(hx.Pred.value_even(), oracle_mod.pred(6, 2, 1, 0, 1)),
+                   (hx.Pred.valid_key(), oracle_mod.pred(8)),
+                   (hx.Pred(hx.PRED_MOD_LT, hx.FIELD_KEY, 7, 3, hx.PRED_NEGATE), oracle_mod.pred(1, 1, 7, 3, 2))]:
+        c = hx.tools.copy_if(to_dev(arr), out, hp, elem_bytes=eb)
+        want = oracle_mod.copy_if(arr, eb, op)
+        assert 2 * c == len(want)
+        np.testing.assert_array_equal(from_dev(out, dt)[: 2 * c], want)
+
+
+def test_copy_if_capacity_and_device_count(hx, oracle_mod):
+    import torch
+    x = np.arange(10000, dtype=np.uint32)
+    out = to_dev(np.zeros(100, np.uint32))
+    c = hx.tools.copy_if(to_dev(x), out, hx.Pred.even(), capacity=100)
+    assert c == 5000  # the full count is reported; only 100 written
+    np.testing.assert_array_equal(from_dev(out, np.uint32), np.arange(0, 200, 2, dtype=np.uint32))
+    dc = torch.zeros(1, dtype=torch.int64, device="cuda")
+    big = to_dev(np.zeros(10000, np.uint32))
+    assert hx.tools.copy_if(to_dev(x), big, hx.Pred.even(), d_count=dc) == -1
+    torch.cuda.synchronize()
+    assert int(dc.item()) == 5000
+
+
+def test_copy_if_empty_input(hx):
+    import torch
+    e = torch.zeros(0, dtype=torch.int32, device="cuda")
+    assert hx.tools.copy_if(e, e, hx.Pred.even()) == 0
