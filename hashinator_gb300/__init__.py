@@ -86,7 +86,7 @@ _SIGS = {
     "hx_get_info": [ctypes.c_void_p, ctypes.POINTER(Info), ctypes.c_void_p],
     "hx_peek_status": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p],
     "hx_bucket_data": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64)],
-    "hx_map_set_tuning": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int],
+    "hx_map_set_tuning": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int],
     "hx_scratch_bytes": [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
     "hx_exclusive_scan_u32": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
                               ctypes.c_void_p],
@@ -281,8 +281,8 @@ class Hashmap:
     def clear(self, stream=None) -> None:
         _check(self._h.hx_clear(self._m, _stream(stream)), "hx_clear")
 
-    def set_tuning(self, group_width: int = 0, block_size: int = 0) -> None:
-        _check(self._h.hx_map_set_tuning(self._m, group_width, block_size), "hx_map_set_tuning")
+    def set_tuning(self, group_width: int = 0, keys_per_thread: int = 0, block_size: int = 0) -> None:
+        _check(self._h.hx_map_set_tuning(self._m, group_width, keys_per_thread, block_size), "hx_map_set_tuning")
 
     # metadata (synchronous) ----------------------------------------------
     def info(self, stream=None) -> Info:

@@ -102,20 +102,15 @@ __device__ __forceinline__ bool cas_pair(P32* p, uint32_t& ek, uint32_t& ev, uin
   return old == expect;
 }
 __device__ __forceinline__ bool cas_pair(P64* p, uint64_t& ek, uint64_t& ev, uint64_t key, uint64_t val) {
-  unsigned long long olo, ohi;
-  asm volatile(
-      "{\n\t.reg .b128 c, n, o;\n\t"
-      "mov.b128 c, {%2, %3};\n\t"
-      "mov.b128 n, {%4, %5};\n\t"
-      "atom.global.relaxed.gpu.cas.b128 o, [%6], c, n;\n\t"
-      "mov.b128 {%0, %1}, o;\n\t}"
-      : "=l"(olo), "=l"(ohi)
-      : "l"(ek), "l"(ev), "l"(key), "l"(val), "l"(p)
-      : "memory");
-  bool ok = (olo == ek) && (ohi == ev);
-  ek = olo;
-  ev = ohi;
-  return ok;
+  // 128-bit operands as "q" registers: the unpacking of the old value is
+  // left to the compiler, so several CAS can be in flight per thread.
+  const unsigned __int128 c = ((unsigned __int128)ev << 64) | ek;
+  const unsigned __int128 n = ((unsigned __int128)val << 64) | key;
+  unsigned __int128 o;
+  asm volatile("atom.global.relaxed.gpu.cas.b128 %0, [%1], %2, %3;" : "=q"(o) : "l"(p), "q"(c), "q"(n) : "memory");
+  ek = (uint64_t)o;
+  ev = (uint64_t)(o >> 64);
+  return o == c;
 }
 // Overwrite the value of a bucket that already holds the key (the
 // reference's atomicExch on .second, kernels_NVIDIA.h:377,397).

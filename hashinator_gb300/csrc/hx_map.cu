@@ -185,6 +185,163 @@ __global__ void __launch_bounds__(256) k_erase(const typename PairTraits<P>::K* 
   }
 }
 
+// ---- thread-per-key variants: U keys in flight per thread -----------------
+
+// Publish (key, val) into bucket h, which is expected EMPTY. Every EMPTY
+// bucket written by libhx holds value 0, so the first attempt needs no read
+// of the bucket; a different stale value costs one retry.
+template <class P>
+__device__ __forceinline__ bool cas_empty(P* b, typename PairTraits<P>::K& ek, typename PairTraits<P>::V& ev,
+                                          typename PairTraits<P>::K key, typename PairTraits<P>::V val) {
+  ek = PairTraits<P>::EMPTY;
+  ev = 0;
+  return cas_pair(b, ek, ev, key, val);
+}
+
+template <class P, int B, int U, bool PAIRS>
+__global__ void __launch_bounds__(256) k_insert_t1(const typename PairTraits<P>::K* __restrict__ keys,
+                                                   const typename PairTraits<P>::V* __restrict__ vals,
+                                                   const P* __restrict__ pairs, uint64_t n,
+                                                   const unsigned long long* d_n, uint64_t n_cap, P* table,
+                                                   int sp, DInfo* info) {
+  using K = typename PairTraits<P>::K;
+  using V = typename PairTraits<P>::V;
+  constexpr K EMPTY = PairTraits<P>::EMPTY;
+  if (d_n) {
+    const uint64_t dn = *d_n;
+    n = dn < n_cap ? dn : n_cap;
+  }
+  const int lane = threadIdx.x & 31;
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  unsigned ins = 0, maxd = 0;
+  bool fail = false;
+  for (uint64_t base = warp * 32 * U; base < n; base += nwarps * 32 * U) {
+    K key[U];
+    V val[U];
+    bool act[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint64_t i = base + (uint64_t)u * 32 + lane;
+      act[u] = i < n;
+      if (act[u]) {
+        if constexpr (PAIRS) {
+          const P pr = pairs[i];
+          key[u] = pr.first;
+          val[u] = pr.second;
+        } else {
+          key[u] = keys[i];
+          val[u] = vals[i];
+        }
+        act[u] = key[u] != EMPTY && key[u] != PairTraits<P>::TOMB;
+      }
+    }
+    uint32_t h[U];
+    K ek[U];
+    V ev[U];
+    bool ok[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (act[u]) {
+        h[u] = home_slot(key[u], sp);
+        ok[u] = cas_empty<P>(table + h[u], ek[u], ev[u], key[u], val[u]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (!act[u]) continue;
+      bool done = ok[u];
+      if (done) {
+        ++ins;
+        maxd = maxd > 1u ? maxd : 1u;
+        continue;
+      }
+      for (int tries = 0; tries < 8 && ek[u] == EMPTY; ++tries) {  // EMPTY with a stale value
+        if (cas_pair(table + h[u], ek[u], ev[u], key[u], val[u])) {
+          ++ins;
+          maxd = maxd > 1u ? maxd : 1u;
+          done = true;
+          break;
+        }
+      }
+      if (done) continue;
+      if (ek[u] == key[u]) {
+        store_value(table + h[u], val[u]);
+        continue;
+      }
+      unsigned d1 = 0;
+      const int r = insert_t1_rest<P, B>(table, sp, key[u], val[u], h[u], d1);
+      if (r == PR_INSERTED) {
+        ++ins;
+        maxd = d1 > maxd ? d1 : maxd;
+      } else if (r == PR_FAIL) {
+        fail = true;
+      }
+    }
+  }
+  publish_counts(info, ins, maxd, fail, lane);
+}
+
+template <class P, int B, int U, bool PAIRS, bool ERASE>
+__global__ void __launch_bounds__(256) k_find_t1(const typename PairTraits<P>::K* __restrict__ keys,
+                                                 typename PairTraits<P>::V* __restrict__ vals, P* pairs, uint64_t n,
+                                                 P* table, int sp, DInfo* info) {
+  using K = typename PairTraits<P>::K;
+  using V = typename PairTraits<P>::V;
+  const unsigned limit = info->max_probe;
+  const int lane = threadIdx.x & 31;
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  unsigned erased = 0;
+  if (limit) {
+    for (uint64_t base = warp * 32 * U; base < n; base += nwarps * 32 * U) {
+      K key[U];
+      bool act[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const uint64_t i = base + (uint64_t)u * 32 + lane;
+        act[u] = i < n;
+        if (act[u]) {
+          if constexpr (PAIRS) key[u] = pairs[i].first;
+          else key[u] = keys[i];
+          act[u] = key[u] != PairTraits<P>::EMPTY && key[u] != PairTraits<P>::TOMB;
+        }
+      }
+      uint32_t h[U];
+      Window<P, B> w[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (act[u]) {
+          h[u] = home_slot(key[u], sp);
+          load_buckets<B>(table + (h[u] & ~(uint32_t)(B - 1)), w[u].k, w[u].v);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (!act[u]) continue;
+        uint32_t slot;
+        V v;
+        if (find_t1<P, B>(table, sp, key[u], limit, h[u], w[u], slot, v)) {
+          if constexpr (ERASE) {
+            if (cas_key(table + slot, key[u], PairTraits<P>::TOMB)) ++erased;
+          } else {
+            const uint64_t i = base + (uint64_t)u * 32 + lane;
+            if constexpr (PAIRS) pairs[i].second = v;
+            else vals[i] = v;
+          }
+        }
+      }
+    }
+  }
+  if constexpr (ERASE) {
+    erased = __reduce_add_sync(0xffffffffu, erased);
+    if (lane == 0 && erased) {
+      atomicAdd(&info->tombstones, (unsigned long long)erased);
+      atomicAdd(&info->fill, 0ull - (unsigned long long)erased);
+    }
+  }
+}
+
 // device_rehash (hashinator.h:285-336) in one pass: one thread per old
 // bucket inserts its valid pair into the new table.
 template <class P, int B>
@@ -219,7 +376,8 @@ __global__ void __launch_bounds__(256) k_rehash(const P* __restrict__ old_t, uin
 // ---------------------------------------------------------------------------
 
 struct Tuning {
-  int group = 0;   // 0 = default for the pair type
+  int group = 0;   // lanes per key; 0 = default for the pair type
+  int unroll = 4;  // keys in flight per thread when group == 1
   int block = 256;
 };
 
@@ -244,7 +402,7 @@ static inline bool is_p32(const hx_map* m) { return m->key_bytes == 4; }
 static inline uint64_t pair_bytes(const hx_map* m) { return is_p32(m) ? 8 : 16; }
 static inline uint64_t nslots(const hx_map* m) { return 1ull << m->sp; }
 
-static int default_group(bool p32) { return p32 ? 2 : 2; }
+static int default_group(bool p32) { return p32 ? 1 : 1; }
 
 // Probe-group geometry for a table: (G, B) with G*B <= table size.
 struct Geo {
@@ -253,10 +411,12 @@ struct Geo {
 static Geo pick_geo(const hx_map* m) {
   const bool p32 = is_p32(m);
   int G = m->tune.group ? m->tune.group : default_group(p32);
-  int B = p32 ? (G == 1 ? 4 : 2) : (G == 1 ? 2 : 1);
+  if (G == 1) return {1, 0};  // thread-per-key kernels pick their own window
+  int B = p32 ? 2 : 1;
   if ((uint64_t)G * B > nslots(m)) {
-    G = 1;
-    B = 1;
+    // a window larger than the table: the smallest group window that fits
+    if (p32 && nslots(m) >= 4) return {2, 2};
+    return {2, 1};
   }
   return {G, B};
 }
@@ -269,26 +429,42 @@ static unsigned grid_for(F kernel, uint64_t work_threads, int block) {
   return (unsigned)(g ? g : 1);
 }
 
-// Dispatch a kernel template over the compiled (G, B) variants.
+// Dispatch a probe-group kernel template over the compiled (G, B) variants
+// (G >= 2; a table smaller than one window falls back to G = 2, B = 1).
 #define HX_GEO_DISPATCH(P, geo, LAUNCH)                                        \
   do {                                                                         \
     if constexpr (sizeof(P) == 8) {                                            \
-      if (geo.G == 1 && geo.B == 1) { LAUNCH(P, 1, 1); }                       \
-      else if (geo.G == 1) { LAUNCH(P, 1, 4); }                                \
+      if (geo.B == 1) { LAUNCH(P, 2, 1); }                                     \
       else if (geo.G == 2) { LAUNCH(P, 2, 2); }                                \
       else if (geo.G == 4) { LAUNCH(P, 4, 2); }                                \
       else if (geo.G == 8) { LAUNCH(P, 8, 2); }                                \
       else if (geo.G == 16) { LAUNCH(P, 16, 2); }                              \
       else { LAUNCH(P, 32, 2); }                                               \
     } else {                                                                   \
-      if (geo.G == 1 && geo.B == 1) { LAUNCH(P, 1, 1); }                       \
-      else if (geo.G == 1) { LAUNCH(P, 1, 2); }                                \
-      else if (geo.G == 2) { LAUNCH(P, 2, 1); }                                \
+      if (geo.G == 2) { LAUNCH(P, 2, 1); }                                     \
       else if (geo.G == 4) { LAUNCH(P, 4, 1); }                                \
       else if (geo.G == 8) { LAUNCH(P, 8, 1); }                                \
       else if (geo.G == 16) { LAUNCH(P, 16, 1); }                              \
       else { LAUNCH(P, 32, 1); }                                               \
     }                                                                          \
+  } while (0)
+
+// Thread-per-key geometry: B buckets (32 B) per window, U keys per thread.
+// A 2-bucket u32 table uses B = 2 with U = 1.
+#define HX_T1_DISPATCH(P, tsize, U, LAUNCH)                      \
+  do {                                                           \
+    if constexpr (sizeof(P) == 8) {                              \
+      if (tsize < 4) { LAUNCH(P, 2, 1); }                        \
+      else if (U >= 8) { LAUNCH(P, 4, 8); }                      \
+      else if (U >= 4) { LAUNCH(P, 4, 4); }                      \
+      else if (U >= 2) { LAUNCH(P, 4, 2); }                      \
+      else { LAUNCH(P, 4, 1); }                                  \
+    } else {                                                     \
+      if (U >= 8) { LAUNCH(P, 2, 8); }                           \
+      else if (U >= 4) { LAUNCH(P, 2, 4); }                      \
+      else if (U >= 2) { LAUNCH(P, 2, 2); }                      \
+      else { LAUNCH(P, 2, 1); }                                  \
+    }                                                            \
   } while (0)
 
 template <class P>
@@ -298,6 +474,26 @@ static hx_status launch_insert(hx_map* m, const void* keys, const void* vals, co
   using V = typename PairTraits<P>::V;
   const Geo geo = pick_geo(m);
   const int block = m->tune.block;
+  if (geo.G == 1) {
+    const int U = m->tune.unroll;
+#define HX_LAUNCH_INSERT_T1(PP, BB, UU)                                                                          \
+  {                                                                                                              \
+    if (pairs) {                                                                                                 \
+      auto kern = k_insert_t1<PP, BB, UU, true>;                                                                 \
+      kern<<<grid_for(kern, (n + UU - 1) / UU, block), block, 0, s>>>(                                           \
+          nullptr, nullptr, static_cast<const PP*>(pairs), n, d_n, n, static_cast<PP*>(m->buckets), m->sp,        \
+          m->info);                                                                                              \
+    } else {                                                                                                     \
+      auto kern = k_insert_t1<PP, BB, UU, false>;                                                                \
+      kern<<<grid_for(kern, (n + UU - 1) / UU, block), block, 0, s>>>(                                           \
+          static_cast<const K*>(keys), static_cast<const V*>(vals), nullptr, n, d_n, n,                          \
+          static_cast<PP*>(m->buckets), m->sp, m->info);                                                         \
+    }                                                                                                            \
+  }
+    HX_T1_DISPATCH(P, nslots(m), U, HX_LAUNCH_INSERT_T1);
+#undef HX_LAUNCH_INSERT_T1
+    return after_launch();
+  }
 #define HX_LAUNCH_INSERT(PP, GG, BB)                                                                      \
   {                                                                                                       \
     if (pairs) {                                                                                          \
@@ -317,12 +513,43 @@ static hx_status launch_insert(hx_map* m, const void* keys, const void* vals, co
   return after_launch();
 }
 
-template <class P>
-static hx_status launch_retrieve(hx_map* m, const void* keys, void* vals, void* pairs, uint64_t n, cudaStream_t s) {
+// retrieve (keys or pairs) and erase share the lookup kernels.
+template <class P, bool ERASE>
+static hx_status launch_find(hx_map* m, const void* keys, void* vals, void* pairs, uint64_t n, cudaStream_t s) {
   using K = typename PairTraits<P>::K;
   using V = typename PairTraits<P>::V;
   const Geo geo = pick_geo(m);
   const int block = m->tune.block;
+  if (geo.G == 1) {
+    const int U = m->tune.unroll;
+#define HX_LAUNCH_FIND_T1(PP, BB, UU)                                                                            \
+  {                                                                                                              \
+    if (pairs) {                                                                                                 \
+      auto kern = k_find_t1<PP, BB, UU, true, ERASE>;                                                            \
+      kern<<<grid_for(kern, (n + UU - 1) / UU, block), block, 0, s>>>(nullptr, nullptr, static_cast<PP*>(pairs), \
+                                                                      n, static_cast<PP*>(m->buckets), m->sp,    \
+                                                                      m->info);                                  \
+    } else {                                                                                                     \
+      auto kern = k_find_t1<PP, BB, UU, false, ERASE>;                                                           \
+      kern<<<grid_for(kern, (n + UU - 1) / UU, block), block, 0, s>>>(                                           \
+          static_cast<const K*>(keys), static_cast<V*>(vals), nullptr, n, static_cast<PP*>(m->buckets), m->sp,   \
+          m->info);                                                                                              \
+    }                                                                                                            \
+  }
+    HX_T1_DISPATCH(P, nslots(m), U, HX_LAUNCH_FIND_T1);
+#undef HX_LAUNCH_FIND_T1
+    return after_launch();
+  }
+  if constexpr (ERASE) {
+#define HX_LAUNCH_ERASE(PP, GG, BB)                                                                        \
+  {                                                                                                        \
+    auto kern = k_erase<PP, GG, BB>;                                                                       \
+    kern<<<grid_for(kern, n * GG, block), block, 0, s>>>(static_cast<const K*>(keys), n,                    \
+                                                         static_cast<PP*>(m->buckets), m->sp, m->info);    \
+  }
+    HX_GEO_DISPATCH(P, geo, HX_LAUNCH_ERASE);
+#undef HX_LAUNCH_ERASE
+  } else {
 #define HX_LAUNCH_RETRIEVE(PP, GG, BB)                                                                      \
   {                                                                                                         \
     if (pairs) {                                                                                            \
@@ -336,24 +563,9 @@ static hx_status launch_retrieve(hx_map* m, const void* keys, void* vals, void* 
                                                            m->sp, m->info);                                 \
     }                                                                                                       \
   }
-  HX_GEO_DISPATCH(P, geo, HX_LAUNCH_RETRIEVE);
+    HX_GEO_DISPATCH(P, geo, HX_LAUNCH_RETRIEVE);
 #undef HX_LAUNCH_RETRIEVE
-  return after_launch();
-}
-
-template <class P>
-static hx_status launch_erase(hx_map* m, const void* keys, uint64_t n, cudaStream_t s) {
-  using K = typename PairTraits<P>::K;
-  const Geo geo = pick_geo(m);
-  const int block = m->tune.block;
-#define HX_LAUNCH_ERASE(PP, GG, BB)                                                                        \
-  {                                                                                                        \
-    auto kern = k_erase<PP, GG, BB>;                                                                       \
-    kern<<<grid_for(kern, n * GG, block), block, 0, s>>>(static_cast<const K*>(keys), n,                    \
-                                                         static_cast<PP*>(m->buckets), m->sp, m->info);    \
   }
-  HX_GEO_DISPATCH(P, geo, HX_LAUNCH_ERASE);
-#undef HX_LAUNCH_ERASE
   return after_launch();
 }
 
@@ -532,8 +744,8 @@ hx_status hx_retrieve(hx_map* m, const void* d_keys, void* d_vals, uint64_t n, h
   if (n == 0) return HX_OK;
   if (!d_keys || !d_vals) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  return is_p32(m) ? launch_retrieve<P32>(m, d_keys, d_vals, nullptr, n, s)
-                   : launch_retrieve<P64>(m, d_keys, d_vals, nullptr, n, s);
+  return is_p32(m) ? launch_find<P32, false>(m, d_keys, d_vals, nullptr, n, s)
+                   : launch_find<P64, false>(m, d_keys, d_vals, nullptr, n, s);
 }
 
 hx_status hx_retrieve_pairs(hx_map* m, void* d_pairs, uint64_t n, hx_stream stream) {
@@ -541,8 +753,8 @@ hx_status hx_retrieve_pairs(hx_map* m, void* d_pairs, uint64_t n, hx_stream stre
   if (n == 0) return HX_OK;
   if (!d_pairs) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  return is_p32(m) ? launch_retrieve<P32>(m, nullptr, nullptr, d_pairs, n, s)
-                   : launch_retrieve<P64>(m, nullptr, nullptr, d_pairs, n, s);
+  return is_p32(m) ? launch_find<P32, false>(m, nullptr, nullptr, d_pairs, n, s)
+                   : launch_find<P64, false>(m, nullptr, nullptr, d_pairs, n, s);
 }
 
 hx_status hx_erase(hx_map* m, const void* d_keys, uint64_t n, hx_stream stream) {
@@ -550,7 +762,8 @@ hx_status hx_erase(hx_map* m, const void* d_keys, uint64_t n, hx_stream stream) 
   if (n == 0) return HX_OK;
   if (!d_keys) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  return is_p32(m) ? launch_erase<P32>(m, d_keys, n, s) : launch_erase<P64>(m, d_keys, n, s);
+  return is_p32(m) ? launch_find<P32, true>(m, d_keys, nullptr, nullptr, n, s)
+                   : launch_find<P64, true>(m, d_keys, nullptr, nullptr, n, s);
 }
 
 hx_status hx_clean_tombstones(hx_map* m, hx_stream stream) {
@@ -679,13 +892,18 @@ hx_status hx_bucket_data(hx_map* m, void** d_buckets, uint64_t* bucket_count) {
   return HX_OK;
 }
 
-hx_status hx_map_set_tuning(hx_map* m, int group_width, int block_size) {
+hx_status hx_map_set_tuning(hx_map* m, int group_width, int keys_per_thread, int block_size) {
   if (!m) return HX_ERR_INVALID_ARG;
   if (group_width) {
     if (group_width != 1 && group_width != 2 && group_width != 4 && group_width != 8 && group_width != 16 &&
         group_width != 32)
       return HX_ERR_INVALID_ARG;
     m->tune.group = group_width;
+  }
+  if (keys_per_thread) {
+    if (keys_per_thread != 1 && keys_per_thread != 2 && keys_per_thread != 4 && keys_per_thread != 8)
+      return HX_ERR_INVALID_ARG;
+    m->tune.unroll = keys_per_thread;
   }
   if (block_size) {
     if (block_size % 32 || block_size < 32 || block_size > 256) return HX_ERR_INVALID_ARG;

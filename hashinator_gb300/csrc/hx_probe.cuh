@@ -101,7 +101,10 @@ __device__ __forceinline__ int probe_insert(P* __restrict__ table, int sp, typen
       if (glane == w) {
         const int j = __ffs(ebits) - 1;
         K ek = EMPTY;
-        V ev = vv[j];
+        V ev = 0;
+#pragma unroll
+        for (int t = 0; t < B; ++t)
+          if (t == j) ev = vv[t];
         for (int tries = 0;; ++tries) {
           if (cas_pair(wp + j, ek, ev, key, val)) {
             res = PR_INSERTED;
@@ -170,6 +173,109 @@ __device__ __forceinline__ int probe_find(const P* __restrict__ table, int sp, t
       return w;
     }
     if (group_ballot<G>(gmask, lane, ebits != 0)) return -1;
+  }
+}
+
+
+// ---------------------------------------------------------------------------
+// Thread-per-key probing (probe group of one lane): a thread holds U keys
+// and issues all their first-window loads (or, for insert, their home-bucket
+// CAS) before resolving any of them, so U independent DRAM requests per
+// thread are in flight. A window is B buckets (32 B: one DRAM sector).
+// ---------------------------------------------------------------------------
+template <class P, int B>
+struct Window {
+  typename PairTraits<P>::K k[B];
+  typename PairTraits<P>::V v[B];
+};
+
+// Lookup with the first window (the aligned block holding the home bucket h)
+// already in w. Returns true and the bucket / value on a hit.
+template <class P, int B>
+__device__ __forceinline__ bool find_t1(const P* __restrict__ table, int sp, typename PairTraits<P>::K key,
+                                        unsigned limit, uint32_t h, Window<P, B>& w, uint32_t& slot,
+                                        typename PairTraits<P>::V& val) {
+  constexpr auto EMPTY = PairTraits<P>::EMPTY;
+  const uint32_t tmask = (1u << sp) - 1u;
+  const uint32_t wstart = h & ~(uint32_t)(B - 1);
+  const int first = (int)(h - wstart);
+  for (uint32_t s = 0;; ++s) {
+    const long long d0 = (long long)s * B - first;
+    if (d0 >= (long long)limit) return false;
+    const uint32_t b0 = (wstart + s * (uint32_t)B) & tmask;
+    if (s > 0) load_buckets<B>(table + b0, w.k, w.v);
+    int hit = -1;
+    bool empty = false;
+#pragma unroll
+    for (int j = B - 1; j >= 0; --j) {  // descending: hit ends on the lowest match
+      const long long d = d0 + j;
+      const bool cons = d >= 0 && d < (long long)limit;
+      if (cons && w.k[j] == key) hit = j;
+      if (cons && w.k[j] == EMPTY) empty = true;
+    }
+    if (hit >= 0) {
+      slot = b0 + hit;
+#pragma unroll
+      for (int j = 0; j < B; ++j)
+        if (j == hit) val = w.v[j];
+      return true;
+    }
+    if (empty) return false;
+  }
+}
+
+// Insert after the home bucket h was found taken by another key (or a
+// TOMBSTONE): continue the linear probe at distance 1. Same decisions as
+// probe_insert.
+template <class P, int B>
+__device__ __noinline__ int insert_t1_rest(P* __restrict__ table, int sp, typename PairTraits<P>::K key,
+                                           typename PairTraits<P>::V val, uint32_t h, unsigned& dist1) {
+  using K = typename PairTraits<P>::K;
+  using V = typename PairTraits<P>::V;
+  constexpr K EMPTY = PairTraits<P>::EMPTY;
+  const uint32_t tmask = (1u << sp) - 1u;
+  const long long tsize = (long long)tmask + 1;
+  const uint32_t wstart = h & ~(uint32_t)(B - 1);
+  const int first = (int)(h - wstart);
+  for (uint32_t s = 0;; ++s) {
+    const long long d0 = (long long)s * B - first;
+    if (d0 >= tsize) return PR_FAIL;
+    P* wp = table + ((wstart + s * (uint32_t)B) & tmask);
+    K kk[B];
+    V vv[B];
+    load_buckets<B>(wp, kk, vv);
+    unsigned mbits = 0, ebits = 0;
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const long long d = d0 + j;
+      const bool cons = d >= 1 && d < tsize;
+      if (cons && kk[j] == key) mbits |= 1u << j;
+      if (cons && kk[j] == EMPTY) ebits |= 1u << j;
+    }
+    if (mbits) {
+      store_value(wp + (__ffs(mbits) - 1), val);
+      return PR_UPDATED;
+    }
+    while (ebits) {
+      const int j = __ffs(ebits) - 1;
+      K ek = EMPTY;
+      V ev = 0;
+#pragma unroll
+      for (int t = 0; t < B; ++t)
+        if (t == j) ev = vv[t];
+      for (int tries = 0;; ++tries) {
+        if (cas_pair(wp + j, ek, ev, key, val)) {
+          dist1 = (unsigned)(d0 + j) + 1u;
+          return PR_INSERTED;
+        }
+        if (ek == key) {
+          store_value(wp + j, val);
+          return PR_UPDATED;
+        }
+        if (ek != EMPTY || tries >= 8) break;
+      }
+      ebits &= ~(1u << j);
+    }
   }
 }
 

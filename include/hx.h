@@ -177,11 +177,12 @@ hx_status hx_peek_status(hx_map* map, int32_t* out, hx_stream stream);
 /* expose_bucketdata() (hashinator.h:477-483): the device bucket array. */
 hx_status hx_bucket_data(hx_map* map, void** d_buckets, uint64_t* bucket_count);
 
-/* Probe-group tuning (no reference counterpart: the reference fixes one
- * 32-lane warp per key, hashinator/defaults.h:26-38). group_width in
- * {1,2,4,8,16,32} lanes per key; block_size a multiple of 32 up to 1024;
- * 0 keeps the current value. */
-hx_status hx_map_set_tuning(hx_map* map, int group_width, int block_size);
+/* Probe tuning (no reference counterpart: the reference fixes one 32-lane
+ * warp per key, hashinator/defaults.h:26-38). group_width in
+ * {1,2,4,8,16,32} lanes per key (1 = one thread per key with
+ * keys_per_thread in {1,2,4,8} keys in flight); block_size a multiple of 32
+ * up to 256. 0 keeps the current value. */
+hx_status hx_map_set_tuning(hx_map* map, int group_width, int keys_per_thread, int block_size);
 
 /* ---- split::tools (splitvector/split_tools.h) -------------------------- */
 

@@ -293,22 +293,25 @@ def test_extract_pattern(hx, oracle_mod, w):
     om = oracle_mod.OracleMap(17, w)
     om.insert(keys, vals, 0.0)
     om.erase(e)
-    rules = [(hx.Pred.value_even(), oracle_mod.pred(6, 2, 1, 0, 1)),
-             (hx.Pred.value_even(skip_sentinels=False), oracle_mod.pred(6, 2, 1, 0, 0)),
-             (hx.Pred.key_lt(1 << (8 * w - 3)), oracle_mod.pred(2, 1, 1 << (8 * w - 3))),
-             (hx.Pred.valid_key(), oracle_mod.pred(8)),
-             (hx.Pred.not_home(), oracle_mod.pred(9))]
+    # (rule on device, rule in the oracle, result independent of bucket layout)
+    rules = [(hx.Pred.value_even(), oracle_mod.pred(6, 2, 1, 0, 1), True),
+             (hx.Pred.value_even(skip_sentinels=False), oracle_mod.pred(6, 2, 1, 0, 0), True),
+             (hx.Pred.key_lt(1 << (8 * w - 3)), oracle_mod.pred(2, 1, 1 << (8 * w - 3)), True),
+             (hx.Pred.valid_key(), oracle_mod.pred(8), True),
+             # which key sits in its home bucket depends on insertion order
+             (hx.Pred.not_home(), oracle_mod.pred(9), False)]
     b = bucket_array(m, w)
-    for hp, op in rules:
+    for hp, op, layout_free in rules:
         out = to_dev(np.zeros(2 * (1 << 17), dt))
         c = m.extract_pattern(hp, out)
-        oc, oout = om.extract(op)
-        assert c == oc
         got = from_dev(out, dt).reshape(-1, 2)[:c]
         # (ii) order = the device's own bucket order: the oracle filter over the device buckets
         np.testing.assert_array_equal(got, _filter_buckets(oracle_mod, b, w, op))
-        # (iii) sorted by key equals the oracle's output sorted by key
-        np.testing.assert_array_equal(np.sort(got[:, 0]), np.sort(oout[:, 0]))
+        if layout_free:
+            # (i) count and (iii) sorted-by-key content equal the oracle's
+            oc, oout = om.extract(op)
+            assert c == oc
+            np.testing.assert_array_equal(np.sort(got[:, 0]), np.sort(oout[:, 0]))
     # capacity smaller than the count: count still reported, HX_ERR_CAPACITY swallowed by wrapper
     small = to_dev(np.zeros(2 * 10, dt))
     assert m.extract_pattern(hx.Pred.valid_key(), small, capacity=10) == om.info()["fill"]
