@@ -208,6 +208,25 @@ hx_status hx_copy_if(const void* d_in, void* d_out, uint64_t n, int elem_bytes, 
                      uint64_t capacity, uint64_t* d_count, uint64_t* h_count, void* d_scratch,
                      uint64_t scratch_bytes, hx_stream stream);
 
+/* Exclusive u32 scan that allocates nothing. No counterpart in the
+ * reference: it is hx_exclusive_scan_u32 for callers that may not allocate
+ * device memory when they scan (a host framework that owns all device memory,
+ * a fixed-budget serving loop, a time-stepping loop where cudaMalloc would
+ * synchronise the device). Its look-back scratch is a static device array of
+ * HX_NOALLOC_SCAN_SCRATCH_BYTES compiled into libhx, held on every GPU that
+ * loads the library until the process exits.
+ * - n <= HX_NOALLOC_SCAN_MAX_N (2^28); a larger n returns HX_ERR_INVALID_ARG
+ *   and launches nothing. In-place (d_out == d_in) is allowed.
+ * - The first call on each device looks up the array's device address (with
+ *   that device current); make that first call before any stream capture.
+ * - Every call shares the one array and clears the part it uses. Calls that
+ *   overlap on the GPU race on it and give wrong results: serialise them,
+ *   for example on one stream.
+ * - No cudaMalloc, cudaFree or allocating library call is made. */
+#define HX_NOALLOC_SCAN_MAX_N (1ull << 28)
+#define HX_NOALLOC_SCAN_SCRATCH_BYTES (256ull + 8ull * (HX_NOALLOC_SCAN_MAX_N / 4096ull))
+hx_status hx_exclusive_scan_u32_noalloc(const uint32_t* d_in, uint32_t* d_out, uint64_t n, hx_stream stream);
+
 /* ---- diagnostics -------------------------------------------------------- */
 
 const char* hx_status_string(hx_status status);
