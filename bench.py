@@ -39,8 +39,6 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-SP = 27
-N_KEYS = 1 << 26
 INSERT_BYTES_PER_KEY = {4: 72, 8: 80}
 QUERY_BYTES_PER_KEY = {4: 40, 8: 48}
 METRIC = "insert+query Mkeys/s (u32 keys/values, 2^26 keys, 2^27 buckets, LF 0.5, 50% hit queries)"
@@ -199,7 +197,8 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     hx.lib()
     width = 4
-    n = N_KEYS
+    n = 1 << args.log_keys
+    sp = args.log_keys + 1
     keys, vals, q, _ = workloads.map_workload(n, width, 2026 + rank, erase_frac=0.0)
 
     def to_dev(a):
@@ -208,7 +207,7 @@ def run_ours(args):
     d_keys, d_vals, d_q = to_dev(keys), to_dev(vals), to_dev(q)
     d_out = torch.empty(n, dtype=torch.int32, device=dev)
     stream = torch.cuda.Stream(device=dev)
-    m = hx.Hashmap(SP, width, stream=stream)
+    m = hx.Hashmap(sp, width, stream=stream)
     if args.group:
         m.set_tuning(group_width=args.group)
 
@@ -314,19 +313,21 @@ def run_ours(args):
                            "query": {"ms": round(t_q * 1e3, 3), "Mkeys_s": round(n / t_q / 1e6, 1),
                                      "GB_s": round(q_gbs, 1), "frac": round(q_gbs / peak, 4)},
                            "clear": {"ms": round(t_clear * 1e3, 3),
-                                     "GB_s": round((1 << SP) * 8 / t_clear / 1e9, 1)}}}
+                                     "GB_s": round((1 << sp) * 8 / t_clear / 1e9, 1)}}}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline()
 
     if rank == 0:
-        line = {"metric": METRIC, "value": round(value, 3), "unit": "Mkeys/s", "n_gpus": world,
+        metric = METRIC if args.log_keys == 26 else METRIC.replace("2^26 keys, 2^27", f"2^{args.log_keys} keys, 2^{sp}")
+        line = {"metric": metric, "value": round(value, 3), "unit": "Mkeys/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
                 "data": "synthetic (seeded bijective keys, PCG64 values)",
-                "config": {"workload": "single map u32/u32: clear + insert 2^26 + retrieve 2^26 (50% hit)",
-                           "size_power": SP, "keys": n, "load_factor": 0.5, "parallelism": "replicas",
+                "config": {"workload": f"single map u32/u32: clear + insert 2^{args.log_keys} + retrieve "
+                                       f"2^{args.log_keys} (50% hit)",
+                           "size_power": sp, "keys": n, "load_factor": 0.5, "parallelism": "replicas",
                            "l2": "inputs larger than L2 (1 GiB table, 256 MiB arrays); no flush",
                            "group_width": args.group or "default"},
                 "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
@@ -345,6 +346,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--group", type=int, default=0, help="probe-group width (0 = library default)")
+    ap.add_argument("--log-keys", type=int, default=26, help="log2 of the key count (table: twice as many buckets)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

@@ -87,6 +87,8 @@ _SIGS = {
     "hx_peek_status": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p],
     "hx_bucket_data": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64)],
     "hx_map_set_tuning": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int],
+    "hx_map_set_insert_mode": [ctypes.c_void_p, ctypes.c_int],
+    "hx_set_l2_fetch_granularity": [ctypes.c_int],
     "hx_scratch_bytes": [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
     "hx_exclusive_scan_u32": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
                               ctypes.c_void_p],
@@ -284,6 +286,9 @@ class Hashmap:
     def set_tuning(self, group_width: int = 0, keys_per_thread: int = 0, block_size: int = 0) -> None:
         _check(self._h.hx_map_set_tuning(self._m, group_width, keys_per_thread, block_size), "hx_map_set_tuning")
 
+    def set_insert_mode(self, blind_cas: bool) -> None:
+        _check(self._h.hx_map_set_insert_mode(self._m, 1 if blind_cas else 0), "hx_map_set_insert_mode")
+
     # metadata (synchronous) ----------------------------------------------
     def info(self, stream=None) -> Info:
         inf = Info()
@@ -357,6 +362,11 @@ class tools:
         if st not in (HX_OK, HX_ERR_CAPACITY):
             _check(st, "hx_copy_if")
         return cnt.value
+
+
+def set_l2_fetch_granularity(nbytes: int) -> None:
+    """cudaLimitMaxL2FetchGranularity for this process's context (32/64/128)."""
+    _check(lib().hx_set_l2_fetch_granularity(nbytes), "hx_set_l2_fetch_granularity")
 
 
 def kernel_launch_count() -> int:

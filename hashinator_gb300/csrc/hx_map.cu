@@ -198,7 +198,9 @@ __device__ __forceinline__ bool cas_empty(P* b, typename PairTraits<P>::K& ek, t
   return cas_pair(b, ek, ev, key, val);
 }
 
-template <class P, int B, int U, bool PAIRS>
+// BLIND: CAS the home bucket first without reading it (EMPTY buckets hold
+// (EMPTY, 0)); else load every key's first window, then CAS into it.
+template <class P, int B, int U, bool PAIRS, bool BLIND>
 __global__ void __launch_bounds__(256) k_insert_t1(const typename PairTraits<P>::K* __restrict__ keys,
                                                    const typename PairTraits<P>::V* __restrict__ vals,
                                                    const P* __restrict__ pairs, uint64_t n,
@@ -237,6 +239,29 @@ __global__ void __launch_bounds__(256) k_insert_t1(const typename PairTraits<P>:
       }
     }
     uint32_t h[U];
+    if constexpr (!BLIND) {
+      Window<P, B> w[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (act[u]) {
+          h[u] = home_slot(key[u], sp);
+          load_buckets<B>(table + (h[u] & ~(uint32_t)(B - 1)), w[u].k, w[u].v);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (!act[u]) continue;
+        unsigned d1 = 0;
+        const int r = insert_t1_win<P, B>(table, sp, key[u], val[u], h[u], w[u], d1);
+        if (r == PR_INSERTED) {
+          ++ins;
+          maxd = d1 > maxd ? d1 : maxd;
+        } else if (r == PR_FAIL) {
+          fail = true;
+        }
+      }
+      continue;
+    }
     K ek[U];
     V ev[U];
     bool ok[U];
@@ -379,6 +404,7 @@ struct Tuning {
   int group = 0;   // lanes per key; 0 = default for the pair type
   int unroll = 4;  // keys in flight per thread when group == 1
   int block = 256;
+  bool blind = true;  // thread-per-key insert: CAS the home bucket without reading it first
 };
 
 }  // namespace hx
@@ -476,22 +502,28 @@ static hx_status launch_insert(hx_map* m, const void* keys, const void* vals, co
   const int block = m->tune.block;
   if (geo.G == 1) {
     const int U = m->tune.unroll;
-#define HX_LAUNCH_INSERT_T1(PP, BB, UU)                                                                          \
+#define HX_LAUNCH_INSERT_T1_B(PP, BB, UU, BL)                                                                     \
   {                                                                                                              \
     if (pairs) {                                                                                                 \
-      auto kern = k_insert_t1<PP, BB, UU, true>;                                                                 \
+      auto kern = k_insert_t1<PP, BB, UU, true, BL>;                                                             \
       kern<<<grid_for(kern, (n + UU - 1) / UU, block), block, 0, s>>>(                                           \
           nullptr, nullptr, static_cast<const PP*>(pairs), n, d_n, n, static_cast<PP*>(m->buckets), m->sp,        \
           m->info);                                                                                              \
     } else {                                                                                                     \
-      auto kern = k_insert_t1<PP, BB, UU, false>;                                                                \
+      auto kern = k_insert_t1<PP, BB, UU, false, BL>;                                                            \
       kern<<<grid_for(kern, (n + UU - 1) / UU, block), block, 0, s>>>(                                           \
           static_cast<const K*>(keys), static_cast<const V*>(vals), nullptr, n, d_n, n,                          \
           static_cast<PP*>(m->buckets), m->sp, m->info);                                                         \
     }                                                                                                            \
   }
+#define HX_LAUNCH_INSERT_T1(PP, BB, UU)                   \
+  {                                                       \
+    if (m->tune.blind) HX_LAUNCH_INSERT_T1_B(PP, BB, UU, true) \
+    else HX_LAUNCH_INSERT_T1_B(PP, BB, UU, false)         \
+  }
     HX_T1_DISPATCH(P, nslots(m), U, HX_LAUNCH_INSERT_T1);
 #undef HX_LAUNCH_INSERT_T1
+#undef HX_LAUNCH_INSERT_T1_B
     return after_launch();
   }
 #define HX_LAUNCH_INSERT(PP, GG, BB)                                                                      \
@@ -889,6 +921,18 @@ hx_status hx_bucket_data(hx_map* m, void** d_buckets, uint64_t* bucket_count) {
   if (!valid_map(m)) return HX_ERR_INVALID_ARG;
   if (d_buckets) *d_buckets = m->buckets;
   if (bucket_count) *bucket_count = nslots(m);
+  return HX_OK;
+}
+
+hx_status hx_map_set_insert_mode(hx_map* m, int blind_cas) {
+  if (!m) return HX_ERR_INVALID_ARG;
+  m->tune.blind = blind_cas != 0;
+  return HX_OK;
+}
+
+hx_status hx_set_l2_fetch_granularity(int bytes) {
+  if (bytes != 32 && bytes != 64 && bytes != 128) return HX_ERR_INVALID_ARG;
+  HX_CUDA(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)bytes));
   return HX_OK;
 }
 

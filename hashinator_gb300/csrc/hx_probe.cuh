@@ -279,4 +279,58 @@ __device__ __noinline__ int insert_t1_rest(P* __restrict__ table, int sp, typena
   }
 }
 
+// Insert with the first window (aligned block holding the home bucket h)
+// already loaded into w: the same decisions as probe_insert, starting at
+// distance 0, so the CAS usually lands on a line that is already in L2.
+template <class P, int B>
+__device__ __forceinline__ int insert_t1_win(P* __restrict__ table, int sp, typename PairTraits<P>::K key,
+                                             typename PairTraits<P>::V val, uint32_t h, Window<P, B>& w,
+                                             unsigned& dist1) {
+  using K = typename PairTraits<P>::K;
+  using V = typename PairTraits<P>::V;
+  constexpr K EMPTY = PairTraits<P>::EMPTY;
+  const uint32_t tmask = (1u << sp) - 1u;
+  const long long tsize = (long long)tmask + 1;
+  const uint32_t wstart = h & ~(uint32_t)(B - 1);
+  const int first = (int)(h - wstart);
+  for (uint32_t s = 0;; ++s) {
+    const long long d0 = (long long)s * B - first;
+    if (d0 >= tsize) return PR_FAIL;
+    P* wp = table + ((wstart + s * (uint32_t)B) & tmask);
+    if (s > 0) load_buckets<B>(wp, w.k, w.v);
+    unsigned mbits = 0, ebits = 0;
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const long long d = d0 + j;
+      const bool cons = d >= 0 && d < tsize;
+      if (cons && w.k[j] == key) mbits |= 1u << j;
+      if (cons && w.k[j] == EMPTY) ebits |= 1u << j;
+    }
+    if (mbits) {
+      store_value(wp + (__ffs(mbits) - 1), val);
+      return PR_UPDATED;
+    }
+    while (ebits) {
+      const int j = __ffs(ebits) - 1;
+      K ek = EMPTY;
+      V ev = 0;
+#pragma unroll
+      for (int t = 0; t < B; ++t)
+        if (t == j) ev = w.v[t];
+      for (int tries = 0;; ++tries) {
+        if (cas_pair(wp + j, ek, ev, key, val)) {
+          dist1 = (unsigned)(d0 + j) + 1u;
+          return PR_INSERTED;
+        }
+        if (ek == key) {
+          store_value(wp + j, val);
+          return PR_UPDATED;
+        }
+        if (ek != EMPTY || tries >= 8) break;
+      }
+      ebits &= ~(1u << j);
+    }
+  }
+}
+
 }  // namespace hx

@@ -184,6 +184,17 @@ hx_status hx_bucket_data(hx_map* map, void** d_buckets, uint64_t* bucket_count);
  * up to 256. 0 keeps the current value. */
 hx_status hx_map_set_tuning(hx_map* map, int group_width, int keys_per_thread, int block_size);
 
+/* Thread-per-key insert mode (no reference counterpart): blind_cas != 0
+ * publishes into the home bucket with one CAS before reading anything;
+ * 0 loads each key's first window and CASes into it afterwards. */
+hx_status hx_map_set_insert_mode(hx_map* map, int blind_cas);
+
+/* Maximum L2 fetch granularity of the calling thread's current device
+ * context, 32/64/128 bytes (cudaLimitMaxL2FetchGranularity; a per-process
+ * hint that ends with the process). Random 32-byte bucket sectors waste half
+ * of every 64-byte fetch. No reference counterpart. */
+hx_status hx_set_l2_fetch_granularity(int bytes);
+
 /* ---- split::tools (splitvector/split_tools.h) -------------------------- */
 
 /* Device scratch bytes that hx_exclusive_scan_u32 (op 0) or hx_copy_if
