@@ -258,24 +258,54 @@ def run_ours(args):
     ms_per_step = elapsed / args.steps * 1e3
     value = world * 2 * n * args.steps / elapsed / 1e6
 
-    # ---- end-to-end through the C ABI with pinned host buffers ----------
+    # ---- end-to-end through the public API with pinned host buffers ------
+    # Chunked and pipelined: H2D of chunk c+1 (copy stream) overlaps the insert
+    # of chunk c (compute stream); the queries' D2H of chunk c overlaps the
+    # query of chunk c+1. Every byte of input crosses H2D and every result
+    # crosses D2H inside the timed region.
     e2e = None
     if not args.no_e2e:
         h_keys = torch.from_numpy(keys.view(np.int32)).pin_memory()
         h_vals = torch.from_numpy(vals.view(np.int32)).pin_memory()
         h_q = torch.from_numpy(q.view(np.int32)).pin_memory()
         h_out = torch.empty(n, dtype=torch.int32).pin_memory()
+        copy = torch.cuda.Stream(device=dev)
+        chunks = args.e2e_chunks
+        bounds = [(c * n // chunks, (c + 1) * n // chunks) for c in range(chunks)]
 
         def e2e_step():
-            with torch.cuda.stream(stream):
-                d_keys.copy_(h_keys, non_blocking=True)
-                d_vals.copy_(h_vals, non_blocking=True)
-                d_q.copy_(h_q, non_blocking=True)
             m.clear(stream=stream)
-            m.insert(d_keys, d_vals, target_lf=0.5, stream=stream)
-            m.retrieve(d_q, d_out, stream=stream)
-            with torch.cuda.stream(stream):
-                h_out.copy_(d_out, non_blocking=True)
+            kv_ready, q_ready = [], []
+            with torch.cuda.stream(copy):
+                for a, b in bounds:
+                    d_keys[a:b].copy_(h_keys[a:b], non_blocking=True)
+                    d_vals[a:b].copy_(h_vals[a:b], non_blocking=True)
+                    ev = torch.cuda.Event()
+                    ev.record(copy)
+                    kv_ready.append(ev)
+                for a, b in bounds:
+                    d_q[a:b].copy_(h_q[a:b], non_blocking=True)
+                    ev = torch.cuda.Event()
+                    ev.record(copy)
+                    q_ready.append(ev)
+            for (a, b), ev in zip(bounds, kv_ready):
+                stream.wait_event(ev)
+                m.insert(d_keys[a:b], d_vals[a:b], target_lf=0.5, stream=stream)
+            done = []
+            for (a, b), ev in zip(bounds, q_ready):
+                stream.wait_event(ev)
+                m.retrieve(d_q[a:b], d_out[a:b], stream=stream)
+                ev2 = torch.cuda.Event()
+                ev2.record(stream)
+                done.append(ev2)
+            with torch.cuda.stream(copy):
+                for (a, b), ev in zip(bounds, done):
+                    copy.wait_event(ev)
+                    h_out[a:b].copy_(d_out[a:b], non_blocking=True)
+            # the next step's clear must not overwrite inputs still in flight
+            fin = torch.cuda.Event()
+            fin.record(copy)
+            stream.wait_event(fin)
 
         for _ in range(max(1, args.warmup // 2)):
             e2e_step()
@@ -291,11 +321,28 @@ def run_ours(args):
             t = torch.tensor([e_el], device=dev)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             e_el = float(t.item())
-        # result check of the e2e output against the device-timed output
-        assert np.array_equal(h_out.numpy().view(np.uint32)[:65536], host_out[:65536])
+        # the e2e results equal the device-timed results
+        assert np.array_equal(h_out.numpy().view(np.uint32), host_out)
         e2e = {"value": round(world * 2 * n * args.steps / e_el / 1e6, 3), "unit": "Mkeys/s",
                "h2d_bytes_per_step": 3 * n * width, "d2h_bytes_per_step": n * width,
-               "ms_per_step": round(e_el / args.steps * 1e3, 3)}
+               "ms_per_step": round(e_el / args.steps * 1e3, 3), "chunks": chunks,
+               "api": "hashinator_gb300.Hashmap (libhx C ABI), copy/compute streams overlapped"}
+
+    # ---- random-access ceiling: random 32-byte sector reads over 1 GiB -----
+    rbuf = torch.empty(1 << 30, dtype=torch.uint8, device=dev)
+    rbuf.zero_()
+    n_reads = 1 << 26
+    rts = []
+    for r in range(4):
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        hx.diag_random_sector_reads(rbuf, rbuf.numel(), n_reads, stream=stream)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        if r:
+            rts.append(a0.elapsed_time(a1) / 1e3)
+    rand_sect_s = n_reads / min(rts)
+    del rbuf
 
     peak, peak_kind = measured_peak()
     ins_gbs = INSERT_BYTES_PER_KEY[width] * n / t_ins / 1e9
@@ -303,8 +350,14 @@ def run_ours(args):
     dominant = "insert" if t_ins >= t_q else "query"
     achieved = ins_gbs if dominant == "insert" else q_gbs
     traffic = traffic_from_profiles(f"{dominant}_u32_lf050")
+    dom_keys_s = n / (t_ins if dominant == "insert" else t_q)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
+                "random_access": {"sector_reads_per_s": round(rand_sect_s / 1e9, 2), "unit": "G sectors/s (32 B)",
+                                  "GB_s_useful": round(rand_sect_s * 32 / 1e9, 1),
+                                  "keys_per_sector_read": round(dom_keys_s / rand_sect_s, 3),
+                                  "note": "random 32-byte sector reads over 1 GiB (hx_diag_random_sector_reads); "
+                                          "every probe needs at least one such read"},
                 "kernel": f"k_insert (insert)" if dominant == "insert" else "k_retrieve (query)",
                 "algorithmic_bytes_per_launch": (INSERT_BYTES_PER_KEY if dominant == "insert"
                                                  else QUERY_BYTES_PER_KEY)[width] * n,
@@ -348,6 +401,7 @@ def main():
     ap.add_argument("--group", type=int, default=0, help="probe-group width (0 = library default)")
     ap.add_argument("--log-keys", type=int, default=26, help="log2 of the key count (table: twice as many buckets)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-chunks", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -401,8 +401,8 @@ __global__ void __launch_bounds__(256) k_rehash(const P* __restrict__ old_t, uin
 // ---------------------------------------------------------------------------
 
 struct Tuning {
-  int group = 0;   // lanes per key; 0 = default for the pair type
-  int unroll = 4;  // keys in flight per thread when group == 1
+  int group = 0;   // lanes per key; 0 = automatic policy (auto_policy)
+  int unroll = 1;  // keys in flight per thread when group == 1
   int block = 256;
   bool blind = true;  // thread-per-key insert: CAS the home bucket without reading it first
 };
@@ -428,15 +428,32 @@ static inline bool is_p32(const hx_map* m) { return m->key_bytes == 4; }
 static inline uint64_t pair_bytes(const hx_map* m) { return is_p32(m) ? 8 : 16; }
 static inline uint64_t nslots(const hx_map* m) { return 1ull << m->sp; }
 
-static int default_group(bool p32) { return p32 ? 1 : 1; }
-
-// Probe-group geometry for a table: (G, B) with G*B <= table size.
+// Automatic probe policy (tune.group == 0), from a GB300 sweep over
+// G x keys-per-thread at load factors 0.5 and 0.9 (2^27 buckets):
+//   insert:       one thread per key, blind home CAS, 1 key per thread;
+//   query/erase:  one thread per key with 4 (u32) or 2 (u64) keys in flight
+//                 below load factor 0.7; 32-lane groups above, where misses
+//                 walk long runs and a 256-512 B window per step wins.
 struct Geo {
   int G, B;
 };
-static Geo pick_geo(const hx_map* m) {
+struct Policy {
+  int G, U;
+};
+static Policy auto_policy(const hx_map* m, bool insert) {
+  if (insert) return {1, 1};
+  const double lf = (double)m->fill_ub / (double)nslots(m);
+  if (lf < 0.7) return {1, is_p32(m) ? 4 : 2};
+  return {32, 1};
+}
+static Policy policy(const hx_map* m, bool insert) {
+  if (m->tune.group == 0) return auto_policy(m, insert);
+  return {m->tune.group, m->tune.unroll};
+}
+
+// Probe-group geometry for a table: (G, B) with G*B <= table size.
+static Geo pick_geo(const hx_map* m, int G) {
   const bool p32 = is_p32(m);
-  int G = m->tune.group ? m->tune.group : default_group(p32);
   if (G == 1) return {1, 0};  // thread-per-key kernels pick their own window
   int B = p32 ? 2 : 1;
   if ((uint64_t)G * B > nslots(m)) {
@@ -498,10 +515,11 @@ static hx_status launch_insert(hx_map* m, const void* keys, const void* vals, co
                                const unsigned long long* d_n, cudaStream_t s) {
   using K = typename PairTraits<P>::K;
   using V = typename PairTraits<P>::V;
-  const Geo geo = pick_geo(m);
+  const Policy pol = policy(m, true);
+  const Geo geo = pick_geo(m, pol.G);
   const int block = m->tune.block;
   if (geo.G == 1) {
-    const int U = m->tune.unroll;
+    const int U = pol.U;
 #define HX_LAUNCH_INSERT_T1_B(PP, BB, UU, BL)                                                                     \
   {                                                                                                              \
     if (pairs) {                                                                                                 \
@@ -550,10 +568,11 @@ template <class P, bool ERASE>
 static hx_status launch_find(hx_map* m, const void* keys, void* vals, void* pairs, uint64_t n, cudaStream_t s) {
   using K = typename PairTraits<P>::K;
   using V = typename PairTraits<P>::V;
-  const Geo geo = pick_geo(m);
+  const Policy pol = policy(m, false);
+  const Geo geo = pick_geo(m, pol.G);
   const int block = m->tune.block;
   if (geo.G == 1) {
-    const int U = m->tune.unroll;
+    const int U = pol.U;
 #define HX_LAUNCH_FIND_T1(PP, BB, UU)                                                                            \
   {                                                                                                              \
     if (pairs) {                                                                                                 \

@@ -100,6 +100,38 @@ static hx_status copy_if_t(const void* d_in, void* d_out, uint64_t n, const hx_p
   return HX_OK;
 }
 
+// Random 32-byte sector reads over a buffer of 2^k sectors: the random-access
+// ceiling of the memory system, against which the probe kernels (one random
+// sector per key at least) are judged. U independent reads per thread.
+__device__ __forceinline__ uint64_t diag_mix(uint64_t i) {
+  uint64_t x = i * 0x9E3779B97F4A7C15ull;
+  x ^= x >> 29;
+  x *= 0xBF58476D1CE4E5B9ull;
+  x ^= x >> 32;
+  return x;
+}
+template <int U>
+__global__ void __launch_bounds__(256) k_diag_random_sectors(const unsigned char* __restrict__ buf,
+                                                             uint64_t sect_mask, uint64_t n,
+                                                             unsigned long long* sink) {
+  unsigned long long acc = 0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t groups = (n + U - 1) / U;
+  for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < groups; g += stride) {
+    unsigned long long a[U], b[U], c[U], d[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint64_t sct = diag_mix(g * U + u) & sect_mask;
+      asm volatile("ld.global.cg.v4.u64 {%0,%1,%2,%3}, [%4];"
+                   : "=l"(a[u]), "=l"(b[u]), "=l"(c[u]), "=l"(d[u])
+                   : "l"(buf + sct * 32));
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc += a[u] ^ b[u] ^ c[u] ^ d[u];
+  }
+  if (acc == 0x9E3779B97F4A7C15ull) *sink = acc;  // keeps the loads alive
+}
+
 }  // namespace hx
 
 using namespace hx;
@@ -122,6 +154,20 @@ const char* hx_status_string(hx_status st) {
 int hx_last_cuda_error(void) { return t_last_cuda_error; }
 
 uint64_t hx_kernel_launch_count(void) { return g_launches.load(); }
+
+hx_status hx_diag_random_sector_reads(const void* d_buf, uint64_t bytes, uint64_t n_reads, hx_stream stream) {
+  if (!d_buf || ((uintptr_t)d_buf % 32) || bytes < 64) return HX_ERR_INVALID_ARG;
+  uint64_t nsect = 1;
+  while (nsect * 2 <= bytes / 32) nsect *= 2;  // largest power of two that fits
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  auto kern = k_diag_random_sectors<4>;
+  const unsigned grid = (unsigned)(sm_count() * blocks_per_sm(kern, 256));
+  // The sink is never written unless the xor of all loaded words hits a
+  // 64-bit constant; it points into the buffer's first word.
+  kern<<<grid, 256, 0, s>>>(static_cast<const unsigned char*>(d_buf), nsect - 1, n_reads,
+                            reinterpret_cast<unsigned long long*>(const_cast<void*>(d_buf)));
+  return after_launch();
+}
 
 hx_status hx_scratch_bytes(int op, uint64_t n, uint64_t* bytes) {
   if (!bytes) return HX_ERR_INVALID_ARG;

@@ -241,6 +241,11 @@ hx_status hx_exclusive_scan_u32_noalloc(const uint32_t* d_in, uint32_t* d_out, u
 /* ---- diagnostics -------------------------------------------------------- */
 
 const char* hx_status_string(hx_status status);
+/* Reads n_reads random 32-byte sectors of d_buf (32-byte aligned, bytes >= 64;
+ * the largest power-of-two number of sectors that fits is used). Time it on
+ * the stream to measure the random-access ceiling the probe kernels are
+ * bounded by. No reference counterpart. */
+hx_status hx_diag_random_sector_reads(const void* d_buf, uint64_t bytes, uint64_t n_reads, hx_stream stream);
 /* The last cudaError_t value seen by the library on this host thread. */
 int hx_last_cuda_error(void);
 /* Number of kernels libhx has launched in this process. */

@@ -11,6 +11,14 @@ from hashinator_gb300 import workloads
 pytestmark = pytest.mark.gpu
 
 GROUPS = [1, 2, 4, 8, 16, 32]
+# (group width, keys per thread, blind insert CAS); group 0 = automatic policy
+TUNINGS = [(0, 0, True), (1, 1, True), (1, 2, False), (1, 4, True), (1, 8, False), (2, 1, True), (4, 1, False),
+           (8, 1, True), (16, 1, True), (32, 1, True)]
+
+
+def _tune(m, t):
+    m.set_tuning(group_width=t[0], keys_per_thread=t[1])
+    m.set_insert_mode(t[2])
 FILL = {4: 0xA5A5A5A5, 8: 0xA5A5A5A5A5A5A5A5}
 
 
@@ -18,14 +26,14 @@ def _dt(w):
     return np.uint32 if w == 4 else np.uint64
 
 
-@pytest.mark.parametrize("group", GROUPS)
+@pytest.mark.parametrize("tuning", TUNINGS)
 @pytest.mark.parametrize("name", golden_cases())
-def test_golden_parity(hx, name, group):
+def test_golden_parity(hx, name, tuning):
     g = load_golden(name)
     w, sp = int(g["key_bytes"]), int(g["size_power"])
     dt = _dt(w)
     m = hx.Hashmap(sp, w)
-    m.set_tuning(group_width=group)
+    _tune(m, tuning)
     m.insert(to_dev(g["keys"]), to_dev(g["vals"]), target_lf=0.0)
     inf = m.info()
     assert inf.fill == int(g["size_after_insert"])
@@ -48,11 +56,11 @@ def test_golden_parity(hx, name, group):
     m.close()
 
 
-def _run_cycle(hx, oracle_mod, w, sp, n, group, seed, erase_frac=0.3, hit=0.5, target_lf=0.0):
+def _run_cycle(hx, oracle_mod, w, sp, n, tuning, seed, erase_frac=0.3, hit=0.5, target_lf=0.0):
     dt = _dt(w)
     keys, vals, q, e = workloads.map_workload(n, w, seed, hit_frac=hit, erase_frac=erase_frac)
     m = hx.Hashmap(sp, w)
-    m.set_tuning(group_width=group)
+    _tune(m, tuning)
     om = oracle_mod.OracleMap(sp, w)
     m.insert(to_dev(keys), to_dev(vals), target_lf=target_lf)
     assert om.insert(keys, vals, target_lf) == 0
@@ -98,19 +106,19 @@ def _run_cycle(hx, oracle_mod, w, sp, n, group, seed, erase_frac=0.3, hit=0.5, t
 
 
 @pytest.mark.parametrize("w", [4, 8])
-@pytest.mark.parametrize("group", GROUPS)
+@pytest.mark.parametrize("tuning", TUNINGS)
 @pytest.mark.parametrize("lf", [0.5, 0.75, 0.9])
-def test_oracle_parity_cycle(hx, oracle_mod, w, group, lf):
+def test_oracle_parity_cycle(hx, oracle_mod, w, tuning, lf):
     sp = 16
     n = int(lf * (1 << sp))
-    _run_cycle(hx, oracle_mod, w, sp, n, group, seed=100 + group)
+    _run_cycle(hx, oracle_mod, w, sp, n, tuning, seed=100 + tuning[0] + 7 * tuning[1])
 
 
 @pytest.mark.parametrize("w", [4, 8])
 def test_oracle_parity_cycle_large(hx, oracle_mod, w):
     """cfg1 shape in full: 2^20 keys, size power 21, 2^21 queries 50/50, erase 25%."""
     sp, n = 21, 1 << 20
-    _run_cycle(hx, oracle_mod, w, sp, n, 0, seed=7, erase_frac=0.25)
+    _run_cycle(hx, oracle_mod, w, sp, n, (0, 0, True), seed=7, erase_frac=0.25)
 
 
 @pytest.mark.parametrize("w", [4, 8])
@@ -131,11 +139,11 @@ def test_growth_rule_matches_reference(hx, oracle_mod, w):
 
 
 @pytest.mark.parametrize("w", [4, 8])
-@pytest.mark.parametrize("group", [1, 2, 32])
-def test_overflow_sets_fail(hx, w, group):
+@pytest.mark.parametrize("tuning", TUNINGS)
+def test_overflow_sets_fail(hx, w, tuning):
     keys = workloads.distinct_keys(20, w, 3)
     m = hx.Hashmap(4, w)
-    m.set_tuning(group_width=group)
+    _tune(m, tuning)
     m.insert(to_dev(keys), to_dev(keys), target_lf=0.0)
     assert m.peek_status() == hx.STATUS_FAIL
     assert m.info().fill == 16
@@ -183,9 +191,9 @@ def test_tiny_tables(hx, oracle_mod, w, sp):
     n = (1 << sp) - 1 if sp > 1 else 1
     keys = workloads.distinct_keys(n, w, 40 + sp)
     vals = workloads.values(n, w, 40 + sp)
-    for group in GROUPS:
+    for tuning in TUNINGS:
         m = hx.Hashmap(sp, w)
-        m.set_tuning(group_width=group)
+        _tune(m, tuning)
         m.insert(to_dev(keys), to_dev(vals), 0.0)
         assert m.peek_status() == hx.STATUS_SUCCESS
         out = full_dev(n, 0, w)
