@@ -88,6 +88,7 @@ _SIGS = {
     "hx_bucket_data": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64)],
     "hx_map_set_tuning": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int],
     "hx_map_set_insert_mode": [ctypes.c_void_p, ctypes.c_int],
+    "hx_map_set_window_bytes": [ctypes.c_void_p, ctypes.c_int],
     "hx_set_l2_fetch_granularity": [ctypes.c_int],
     "hx_diag_random_sector_reads": [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p],
     "hx_scratch_bytes": [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
@@ -286,6 +287,9 @@ class Hashmap:
 
     def set_tuning(self, group_width: int = 0, keys_per_thread: int = 0, block_size: int = 0) -> None:
         _check(self._h.hx_map_set_tuning(self._m, group_width, keys_per_thread, block_size), "hx_map_set_tuning")
+
+    def set_window_bytes(self, nbytes: int) -> None:
+        _check(self._h.hx_map_set_window_bytes(self._m, nbytes), "hx_map_set_window_bytes")
 
     def set_insert_mode(self, blind_cas: bool) -> None:
         _check(self._h.hx_map_set_insert_mode(self._m, 1 if blind_cas else 0), "hx_map_set_insert_mode")

@@ -54,9 +54,9 @@ __host__ __device__ __forceinline__ uint32_t home_slot(K key, int sp) {
   return (uint32_t)fib_hash(key, sp) & ((1u << sp) - 1u);
 }
 
-// ---- bucket loads: B consecutive buckets per lane in one vector access ----
-// 8 B (u32 pair, B=1), 16 B (B=2 u32 pairs or B=1 u64 pair) or 32 B
-// (B=4 u32 pairs or B=2 u64 pairs, the sm_100+ 256-bit load).
+// ---- bucket loads: B consecutive buckets per lane in vector accesses ------
+// 8 B (u32 pair, B=1), 16 B (B=2 u32 pairs or B=1 u64 pair), 32 B (B=4 u32
+// pairs or B=2 u64 pairs, the sm_100+ 256-bit load) or 64 B (two of those).
 template <int B>
 __device__ __forceinline__ void load_buckets(const P32* p, uint32_t (&k)[B], uint32_t (&v)[B]) {
   if constexpr (B == 1) {
@@ -66,14 +66,17 @@ __device__ __forceinline__ void load_buckets(const P32* p, uint32_t (&k)[B], uin
     uint4 x = __ldcg(reinterpret_cast<const uint4*>(p));
     k[0] = x.x; v[0] = x.y; k[1] = x.z; v[1] = x.w;
   } else {
-    static_assert(B == 4, "B in {1,2,4}");
-    unsigned long long a, b, c, d;
-    asm volatile("ld.global.cg.v4.u64 {%0,%1,%2,%3}, [%4];"
-                 : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(p));
-    k[0] = (uint32_t)a; v[0] = (uint32_t)(a >> 32);
-    k[1] = (uint32_t)b; v[1] = (uint32_t)(b >> 32);
-    k[2] = (uint32_t)c; v[2] = (uint32_t)(c >> 32);
-    k[3] = (uint32_t)d; v[3] = (uint32_t)(d >> 32);
+    static_assert(B == 4 || B == 8, "B in {1,2,4,8}");
+#pragma unroll
+    for (int h = 0; h < B / 4; ++h) {
+      unsigned long long a, b, c, d;
+      asm volatile("ld.global.cg.v4.u64 {%0,%1,%2,%3}, [%4];"
+                   : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(p + 4 * h));
+      k[4 * h + 0] = (uint32_t)a; v[4 * h + 0] = (uint32_t)(a >> 32);
+      k[4 * h + 1] = (uint32_t)b; v[4 * h + 1] = (uint32_t)(b >> 32);
+      k[4 * h + 2] = (uint32_t)c; v[4 * h + 2] = (uint32_t)(c >> 32);
+      k[4 * h + 3] = (uint32_t)d; v[4 * h + 3] = (uint32_t)(d >> 32);
+    }
   }
 }
 template <int B>
@@ -82,11 +85,14 @@ __device__ __forceinline__ void load_buckets(const P64* p, uint64_t (&k)[B], uin
     ulonglong2 x = __ldcg(reinterpret_cast<const ulonglong2*>(p));
     k[0] = x.x; v[0] = x.y;
   } else {
-    static_assert(B == 2, "B in {1,2}");
-    unsigned long long a, b, c, d;
-    asm volatile("ld.global.cg.v4.u64 {%0,%1,%2,%3}, [%4];"
-                 : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(p));
-    k[0] = a; v[0] = b; k[1] = c; v[1] = d;
+    static_assert(B == 2 || B == 4, "B in {1,2,4}");
+#pragma unroll
+    for (int h = 0; h < B / 2; ++h) {
+      unsigned long long a, b, c, d;
+      asm volatile("ld.global.cg.v4.u64 {%0,%1,%2,%3}, [%4];"
+                   : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(p + 2 * h));
+      k[2 * h] = a; v[2 * h] = b; k[2 * h + 1] = c; v[2 * h + 1] = d;
+    }
   }
 }
 

@@ -405,6 +405,7 @@ struct Tuning {
   int unroll = 1;  // keys in flight per thread when group == 1
   int block = 256;
   bool blind = true;  // thread-per-key insert: CAS the home bucket without reading it first
+  bool wide = false;  // thread-per-key windows of 64 B instead of 32 B
 };
 
 }  // namespace hx
@@ -494,16 +495,26 @@ static unsigned grid_for(F kernel, uint64_t work_threads, int block) {
 
 // Thread-per-key geometry: B buckets (32 B) per window, U keys per thread.
 // A 2-bucket u32 table uses B = 2 with U = 1.
-#define HX_T1_DISPATCH(P, tsize, U, LAUNCH)                      \
+#define HX_T1_DISPATCH(P, tsize, U, WIDE, LAUNCH)                \
   do {                                                           \
     if constexpr (sizeof(P) == 8) {                              \
       if (tsize < 4) { LAUNCH(P, 2, 1); }                        \
+      else if (WIDE && tsize >= 8) {                             \
+        if (U >= 4) { LAUNCH(P, 8, 4); }                         \
+        else if (U >= 2) { LAUNCH(P, 8, 2); }                    \
+        else { LAUNCH(P, 8, 1); }                                \
+      }                                                          \
       else if (U >= 8) { LAUNCH(P, 4, 8); }                      \
       else if (U >= 4) { LAUNCH(P, 4, 4); }                      \
       else if (U >= 2) { LAUNCH(P, 4, 2); }                      \
       else { LAUNCH(P, 4, 1); }                                  \
     } else {                                                     \
-      if (U >= 8) { LAUNCH(P, 2, 8); }                           \
+      if (WIDE && tsize >= 4) {                                  \
+        if (U >= 4) { LAUNCH(P, 4, 4); }                         \
+        else if (U >= 2) { LAUNCH(P, 4, 2); }                    \
+        else { LAUNCH(P, 4, 1); }                                \
+      }                                                          \
+      else if (U >= 8) { LAUNCH(P, 2, 8); }                      \
       else if (U >= 4) { LAUNCH(P, 2, 4); }                      \
       else if (U >= 2) { LAUNCH(P, 2, 2); }                      \
       else { LAUNCH(P, 2, 1); }                                  \
@@ -539,7 +550,7 @@ static hx_status launch_insert(hx_map* m, const void* keys, const void* vals, co
     if (m->tune.blind) HX_LAUNCH_INSERT_T1_B(PP, BB, UU, true) \
     else HX_LAUNCH_INSERT_T1_B(PP, BB, UU, false)         \
   }
-    HX_T1_DISPATCH(P, nslots(m), U, HX_LAUNCH_INSERT_T1);
+    HX_T1_DISPATCH(P, nslots(m), U, m->tune.wide, HX_LAUNCH_INSERT_T1);
 #undef HX_LAUNCH_INSERT_T1
 #undef HX_LAUNCH_INSERT_T1_B
     return after_launch();
@@ -587,7 +598,7 @@ static hx_status launch_find(hx_map* m, const void* keys, void* vals, void* pair
           m->info);                                                                                              \
     }                                                                                                            \
   }
-    HX_T1_DISPATCH(P, nslots(m), U, HX_LAUNCH_FIND_T1);
+    HX_T1_DISPATCH(P, nslots(m), U, m->tune.wide, HX_LAUNCH_FIND_T1);
 #undef HX_LAUNCH_FIND_T1
     return after_launch();
   }
@@ -946,6 +957,12 @@ hx_status hx_bucket_data(hx_map* m, void** d_buckets, uint64_t* bucket_count) {
 hx_status hx_map_set_insert_mode(hx_map* m, int blind_cas) {
   if (!m) return HX_ERR_INVALID_ARG;
   m->tune.blind = blind_cas != 0;
+  return HX_OK;
+}
+
+hx_status hx_map_set_window_bytes(hx_map* m, int bytes) {
+  if (!m || (bytes != 32 && bytes != 64)) return HX_ERR_INVALID_ARG;
+  m->tune.wide = bytes == 64;
   return HX_OK;
 }
 

@@ -189,6 +189,10 @@ hx_status hx_map_set_tuning(hx_map* map, int group_width, int keys_per_thread, i
  * 0 loads each key's first window and CASes into it afterwards. */
 hx_status hx_map_set_insert_mode(hx_map* map, int blind_cas);
 
+/* Thread-per-key window: 32 (one DRAM sector) or 64 bytes of buckets per
+ * probe step. No reference counterpart. */
+hx_status hx_map_set_window_bytes(hx_map* map, int bytes);
+
 /* Maximum L2 fetch granularity of the calling thread's current device
  * context, 32/64/128 bytes (cudaLimitMaxL2FetchGranularity; a per-process
  * hint that ends with the process). Random 32-byte bucket sectors waste half

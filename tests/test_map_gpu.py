@@ -11,14 +11,16 @@ from hashinator_gb300 import workloads
 pytestmark = pytest.mark.gpu
 
 GROUPS = [1, 2, 4, 8, 16, 32]
-# (group width, keys per thread, blind insert CAS); group 0 = automatic policy
-TUNINGS = [(0, 0, True), (1, 1, True), (1, 2, False), (1, 4, True), (1, 8, False), (2, 1, True), (4, 1, False),
-           (8, 1, True), (16, 1, True), (32, 1, True)]
+# (group width, keys per thread, blind insert CAS, window bytes); group 0 = automatic policy
+TUNINGS = [(0, 0, True, 32), (1, 1, True, 32), (1, 2, False, 32), (1, 4, True, 32), (1, 8, False, 32),
+           (1, 1, True, 64), (1, 2, False, 64), (1, 4, True, 64), (2, 1, True, 32), (4, 1, False, 32),
+           (8, 1, True, 32), (16, 1, True, 32), (32, 1, True, 32)]
 
 
 def _tune(m, t):
     m.set_tuning(group_width=t[0], keys_per_thread=t[1])
     m.set_insert_mode(t[2])
+    m.set_window_bytes(t[3])
 FILL = {4: 0xA5A5A5A5, 8: 0xA5A5A5A5A5A5A5A5}
 
 
@@ -111,14 +113,14 @@ def _run_cycle(hx, oracle_mod, w, sp, n, tuning, seed, erase_frac=0.3, hit=0.5, 
 def test_oracle_parity_cycle(hx, oracle_mod, w, tuning, lf):
     sp = 16
     n = int(lf * (1 << sp))
-    _run_cycle(hx, oracle_mod, w, sp, n, tuning, seed=100 + tuning[0] + 7 * tuning[1])
+    _run_cycle(hx, oracle_mod, w, sp, n, tuning, seed=100 + tuning[0] + 7 * tuning[1] + tuning[3])
 
 
 @pytest.mark.parametrize("w", [4, 8])
 def test_oracle_parity_cycle_large(hx, oracle_mod, w):
     """cfg1 shape in full: 2^20 keys, size power 21, 2^21 queries 50/50, erase 25%."""
     sp, n = 21, 1 << 20
-    _run_cycle(hx, oracle_mod, w, sp, n, (0, 0, True), seed=7, erase_frac=0.25)
+    _run_cycle(hx, oracle_mod, w, sp, n, (0, 0, True, 32), seed=7, erase_frac=0.25)
 
 
 @pytest.mark.parametrize("w", [4, 8])
