@@ -328,20 +328,22 @@ def run_ours(args):
                "ms_per_step": round(e_el / args.steps * 1e3, 3), "chunks": chunks,
                "api": "hashinator_gb300.Hashmap (libhx C ABI), copy/compute streams overlapped"}
 
-    # ---- random-access ceiling: random 32-byte sector reads over 1 GiB -----
+    # ---- random-access ceilings over 1 GiB: 32-byte sector reads, 64-bit CAS -
     rbuf = torch.empty(1 << 30, dtype=torch.uint8, device=dev)
-    rbuf.zero_()
-    n_reads = 1 << 26
-    rts = []
-    for r in range(4):
-        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a0.record(stream)
-        hx.diag_random_sector_reads(rbuf, rbuf.numel(), n_reads, stream=stream)
-        a1.record(stream)
-        torch.cuda.synchronize()
-        if r:
-            rts.append(a0.elapsed_time(a1) / 1e3)
-    rand_sect_s = n_reads / min(rts)
+    n_ops = 1 << 26
+    ceil = {}
+    for mode in (0, 1):
+        rts = []
+        for r in range(4):
+            rbuf.zero_()
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a0.record(stream)
+            hx.diag_random_access(rbuf, rbuf.numel(), n_ops, mode, stream=stream)
+            a1.record(stream)
+            torch.cuda.synchronize()
+            if r:
+                rts.append(a0.elapsed_time(a1) / 1e3)
+        ceil[mode] = n_ops / min(rts)
     del rbuf
 
     peak, peak_kind = measured_peak()
@@ -353,12 +355,13 @@ def run_ours(args):
     dom_keys_s = n / (t_ins if dominant == "insert" else t_q)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
-                "random_access": {"sector_reads_per_s": round(rand_sect_s / 1e9, 2), "unit": "G sectors/s (32 B)",
-                                  "GB_s_useful": round(rand_sect_s * 32 / 1e9, 1),
-                                  "keys_per_sector_read": round(dom_keys_s / rand_sect_s, 3),
-                                  "note": "random 32-byte sector reads over 1 GiB (hx_diag_random_sector_reads); "
-                                          "every probe needs at least one such read"},
-                "kernel": f"k_insert (insert)" if dominant == "insert" else "k_retrieve (query)",
+                "random_access": {
+                    "read32_G_per_s": round(ceil[0] / 1e9, 2), "cas64_G_per_s": round(ceil[1] / 1e9, 2),
+                    "frac": round(dom_keys_s / (ceil[1] if dominant == "insert" else ceil[0]), 3),
+                    "note": "ceilings measured in this run by hx_diag_random_access over 1 GiB; frac = keys/s of the "
+                            "dominant kernel over the ceiling of its one unavoidable random op per key (CAS for "
+                            "insert, 32-byte read for query); DRAM transactions, not bytes, bound these kernels"},
+                "kernel": "k_insert_t1 (insert)" if dominant == "insert" else "k_find_t1 (query)",
                 "algorithmic_bytes_per_launch": (INSERT_BYTES_PER_KEY if dominant == "insert"
                                                  else QUERY_BYTES_PER_KEY)[width] * n,
                 "per_op": {"insert": {"ms": round(t_ins * 1e3, 3), "Mkeys_s": round(n / t_ins / 1e6, 1),

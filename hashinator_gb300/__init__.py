@@ -90,7 +90,7 @@ _SIGS = {
     "hx_map_set_insert_mode": [ctypes.c_void_p, ctypes.c_int],
     "hx_map_set_window_bytes": [ctypes.c_void_p, ctypes.c_int],
     "hx_set_l2_fetch_granularity": [ctypes.c_int],
-    "hx_diag_random_sector_reads": [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p],
+    "hx_diag_random_access": [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p],
     "hx_scratch_bytes": [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
     "hx_exclusive_scan_u32": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
                               ctypes.c_void_p],
@@ -374,10 +374,10 @@ def set_l2_fetch_granularity(nbytes: int) -> None:
     _check(lib().hx_set_l2_fetch_granularity(nbytes), "hx_set_l2_fetch_granularity")
 
 
-def diag_random_sector_reads(buf, nbytes: int, n_reads: int, stream=None) -> None:
-    """Launch n_reads random 32-byte sector reads over a device buffer."""
-    _check(lib().hx_diag_random_sector_reads(_ptr(buf), nbytes, n_reads, _stream(stream)),
-           "hx_diag_random_sector_reads")
+def diag_random_access(buf, nbytes: int, n_ops: int, mode: int = 0, stream=None) -> None:
+    """Launch n_ops random 32-byte sector reads (mode 0) or 64-bit CAS
+    (mode 1) over a device buffer: the random-access ceilings."""
+    _check(lib().hx_diag_random_access(_ptr(buf), nbytes, n_ops, mode, _stream(stream)), "hx_diag_random_access")
 
 
 def kernel_launch_count() -> int:

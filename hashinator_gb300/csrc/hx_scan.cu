@@ -131,6 +131,16 @@ __global__ void __launch_bounds__(256) k_diag_random_sectors(const unsigned char
   }
   if (acc == 0x9E3779B97F4A7C15ull) *sink = acc;  // keeps the loads alive
 }
+// Random 64-bit CAS on word 0 of random 32-byte sectors: the ceiling of the
+// insert kernels, which publish each new pair with one CAS.
+__global__ void __launch_bounds__(256) k_diag_random_cas(unsigned long long* __restrict__ buf, uint64_t sect_mask,
+                                                         uint64_t n, unsigned long long* sink) {
+  unsigned long long acc = 0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+    acc += atomicCAS(buf + (diag_mix(i) & sect_mask) * 4, 0ull, (unsigned long long)i + 1);
+  if (acc == 0x9E3779B97F4A7C15ull) *sink = acc;
+}
 
 }  // namespace hx
 
@@ -155,17 +165,22 @@ int hx_last_cuda_error(void) { return t_last_cuda_error; }
 
 uint64_t hx_kernel_launch_count(void) { return g_launches.load(); }
 
-hx_status hx_diag_random_sector_reads(const void* d_buf, uint64_t bytes, uint64_t n_reads, hx_stream stream) {
-  if (!d_buf || ((uintptr_t)d_buf % 32) || bytes < 64) return HX_ERR_INVALID_ARG;
+hx_status hx_diag_random_access(void* d_buf, uint64_t bytes, uint64_t n_ops, int mode, hx_stream stream) {
+  if (!d_buf || ((uintptr_t)d_buf % 32) || bytes < 64 || (mode != 0 && mode != 1)) return HX_ERR_INVALID_ARG;
   uint64_t nsect = 1;
   while (nsect * 2 <= bytes / 32) nsect *= 2;  // largest power of two that fits
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  auto kern = k_diag_random_sectors<4>;
-  const unsigned grid = (unsigned)(sm_count() * blocks_per_sm(kern, 256));
-  // The sink is never written unless the xor of all loaded words hits a
-  // 64-bit constant; it points into the buffer's first word.
-  kern<<<grid, 256, 0, s>>>(static_cast<const unsigned char*>(d_buf), nsect - 1, n_reads,
-                            reinterpret_cast<unsigned long long*>(const_cast<void*>(d_buf)));
+  // The sink is never written unless an accumulated 64-bit sum hits a fixed
+  // constant; it points at the buffer's first word.
+  unsigned long long* sink = static_cast<unsigned long long*>(d_buf);
+  if (mode == 0) {
+    auto kern = k_diag_random_sectors<4>;
+    const unsigned grid = (unsigned)(sm_count() * blocks_per_sm(kern, 256));
+    kern<<<grid, 256, 0, s>>>(static_cast<const unsigned char*>(d_buf), nsect - 1, n_ops, sink);
+  } else {
+    const unsigned grid = (unsigned)(sm_count() * blocks_per_sm(k_diag_random_cas, 256));
+    k_diag_random_cas<<<grid, 256, 0, s>>>(static_cast<unsigned long long*>(d_buf), nsect - 1, n_ops, sink);
+  }
   return after_launch();
 }
 

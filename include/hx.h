@@ -245,11 +245,12 @@ hx_status hx_exclusive_scan_u32_noalloc(const uint32_t* d_in, uint32_t* d_out, u
 /* ---- diagnostics -------------------------------------------------------- */
 
 const char* hx_status_string(hx_status status);
-/* Reads n_reads random 32-byte sectors of d_buf (32-byte aligned, bytes >= 64;
- * the largest power-of-two number of sectors that fits is used). Time it on
- * the stream to measure the random-access ceiling the probe kernels are
- * bounded by. No reference counterpart. */
-hx_status hx_diag_random_sector_reads(const void* d_buf, uint64_t bytes, uint64_t n_reads, hx_stream stream);
+/* Random-access ceiling probe (no reference counterpart): mode 0 reads
+ * n_ops random 32-byte sectors of d_buf, mode 1 does n_ops random 64-bit CAS
+ * (0 -> nonzero) on word 0 of random sectors, so the buffer is modified.
+ * d_buf is 32-byte aligned, bytes >= 64; the largest power-of-two number of
+ * sectors that fits is used. Time it on the stream. */
+hx_status hx_diag_random_access(void* d_buf, uint64_t bytes, uint64_t n_ops, int mode, hx_stream stream);
 /* The last cudaError_t value seen by the library on this host thread. */
 int hx_last_cuda_error(void);
 /* Number of kernels libhx has launched in this process. */
