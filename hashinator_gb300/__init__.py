@@ -24,8 +24,8 @@ import ctypes
 import os
 from pathlib import Path
 
-__all__ = ["lib", "HXError", "Hashmap", "Pred", "tools", "STATUS_SUCCESS", "STATUS_FAIL", "STATUS_INVALID",
-           "LIB_PATH", "Info"]
+__all__ = ["lib", "HXError", "Hashmap", "Pred", "tools", "Batch", "BatchPlan", "STATUS_SUCCESS", "STATUS_FAIL",
+           "STATUS_INVALID", "LIB_PATH", "Info"]
 
 LIB_PATH = Path(__file__).resolve().parent / "libhx.so"
 
@@ -68,6 +68,15 @@ class _CPred(ctypes.Structure):
                 ("reserved", ctypes.c_uint32), ("a", ctypes.c_uint64), ("b", ctypes.c_uint64)]
 
 
+class _CBatchWork(ctypes.Structure):
+    _fields_ = [("ins_keys", ctypes.c_void_p), ("ins_vals", ctypes.c_void_p),
+                ("ins_offsets", ctypes.POINTER(ctypes.c_uint64)),
+                ("query_keys", ctypes.c_void_p), ("query_out", ctypes.c_void_p),
+                ("query_offsets", ctypes.POINTER(ctypes.c_uint64)),
+                ("erase_keys", ctypes.c_void_p), ("erase_offsets", ctypes.POINTER(ctypes.c_uint64)),
+                ("clean", ctypes.c_int)]
+
+
 _lib_handle = None
 
 _SIGS = {
@@ -98,6 +107,23 @@ _SIGS = {
                    ctypes.c_uint64, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.c_void_p,
                    ctypes.c_uint64, ctypes.c_void_p],
 }
+_SIGS.update({
+    "hx_batch_create": [ctypes.POINTER(ctypes.c_void_p), ctypes.c_uint32, ctypes.POINTER(ctypes.c_int32), ctypes.c_int,
+                        ctypes.c_int, ctypes.c_void_p],
+    "hx_batch_destroy": [ctypes.c_void_p],
+    "hx_batch_clear": [ctypes.c_void_p, ctypes.c_void_p],
+    "hx_batch_map_info": [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(Info), ctypes.c_void_p],
+    "hx_batch_bucket_data": [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p),
+                             ctypes.POINTER(ctypes.c_uint64)],
+    "hx_batch_plan_create": [ctypes.c_void_p, ctypes.POINTER(_CBatchWork), ctypes.POINTER(ctypes.c_void_p),
+                             ctypes.c_void_p],
+    "hx_batch_plan_destroy": [ctypes.c_void_p],
+    "hx_batch_set_tuning": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
+    "hx_batch_run": [ctypes.c_void_p, ctypes.c_void_p],
+    "hx_batch_run_graph": [ctypes.c_void_p, ctypes.c_void_p],
+    "hx_batch_run_per_map": [ctypes.c_void_p, ctypes.c_void_p],
+    "hx_batch_check": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p],
+})
 _EXTRA_SIGS = {
     "hx_status_string": ([ctypes.c_int], ctypes.c_char_p),
     "hx_last_cuda_error": ([], ctypes.c_int),
@@ -367,6 +393,111 @@ class tools:
         if st not in (HX_OK, HX_ERR_CAPACITY):
             _check(st, "hx_copy_if")
         return cnt.value
+
+
+def _offsets(offs):
+    if offs is None:
+        return None, None
+    import numpy as _np
+    a = _np.ascontiguousarray(_np.asarray(offs, dtype=_np.uint64))
+    return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+
+
+class Batch:
+    """A directory of many independent maps in one device arena (hx_batch)."""
+
+    def __init__(self, size_powers, key_bytes: int = 4, stream=None):
+        self._h = lib()
+        import numpy as _np
+        sp = _np.ascontiguousarray(_np.asarray(size_powers, dtype=_np.int32))
+        self.n_maps = len(sp)
+        self.size_powers = sp
+        self.key_bytes = key_bytes
+        self._b = ctypes.c_void_p()
+        _check(self._h.hx_batch_create(ctypes.byref(self._b), len(sp), sp.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                       key_bytes, key_bytes, _stream(stream)), "hx_batch_create")
+
+    def close(self) -> None:
+        if self._b and self._b.value:
+            _check(self._h.hx_batch_destroy(self._b), "hx_batch_destroy")
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def clear(self, stream=None) -> None:
+        _check(self._h.hx_batch_clear(self._b, _stream(stream)), "hx_batch_clear")
+
+    def map_info(self, i: int, stream=None) -> Info:
+        inf = Info()
+        _check(self._h.hx_batch_map_info(self._b, i, ctypes.byref(inf), _stream(stream)), "hx_batch_map_info")
+        return inf
+
+    def bucket_data(self, i: int) -> tuple[int, int]:
+        p, n = ctypes.c_void_p(), ctypes.c_uint64()
+        _check(self._h.hx_batch_bucket_data(self._b, i, ctypes.byref(p), ctypes.byref(n)), "hx_batch_bucket_data")
+        return p.value, n.value
+
+    def plan(self, ins_keys=None, ins_vals=None, ins_offsets=None, query_keys=None, query_out=None,
+             query_offsets=None, erase_keys=None, erase_offsets=None, clean: bool = False, stream=None) -> "BatchPlan":
+        return BatchPlan(self, ins_keys, ins_vals, ins_offsets, query_keys, query_out, query_offsets, erase_keys,
+                         erase_offsets, clean, stream)
+
+
+class BatchPlan:
+    """One round of work over a Batch, run as one persistent launch."""
+
+    def __init__(self, batch: Batch, ins_keys, ins_vals, ins_offsets, query_keys, query_out, query_offsets,
+                 erase_keys, erase_offsets, clean, stream):
+        self.batch = batch
+        self._h = batch._h
+        self._keep = (ins_keys, ins_vals, query_keys, query_out, erase_keys)
+        io, iop = _offsets(ins_offsets)
+        qo, qop = _offsets(query_offsets)
+        eo, eop = _offsets(erase_offsets)
+        w = _CBatchWork(_ptr(ins_keys), _ptr(ins_vals), iop, _ptr(query_keys), _ptr(query_out), qop,
+                        _ptr(erase_keys), eop, 1 if clean else 0)
+        self._p = ctypes.c_void_p()
+        _check(self._h.hx_batch_plan_create(batch._b, ctypes.byref(w), ctypes.byref(self._p), _stream(stream)),
+               "hx_batch_plan_create")
+        self.tuning = {"group_width": 1, "block_size": 256, "tile_keys": 2048}
+
+    def close(self) -> None:
+        if self._p and self._p.value:
+            _check(self._h.hx_batch_plan_destroy(self._p), "hx_batch_plan_destroy")
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_tuning(self, group_width: int = 0, block_size: int = 0, tile_keys: int = 0, stream=None) -> None:
+        _check(self._h.hx_batch_set_tuning(self._p, group_width, block_size, tile_keys, _stream(stream)),
+               "hx_batch_set_tuning")
+        for k, v in (("group_width", group_width), ("block_size", block_size), ("tile_keys", tile_keys)):
+            if v:
+                self.tuning[k] = v
+
+    def run(self, stream=None) -> None:
+        _check(self._h.hx_batch_run(self._p, _stream(stream)), "hx_batch_run")
+
+    def run_graph(self, stream=None) -> None:
+        _check(self._h.hx_batch_run_graph(self._p, _stream(stream)), "hx_batch_run_graph")
+
+    def run_per_map(self, stream=None) -> None:
+        _check(self._h.hx_batch_run_per_map(self._p, _stream(stream)), "hx_batch_run_per_map")
+
+    def check(self, stream=None) -> int:
+        e = ctypes.c_int32()
+        st = self._h.hx_batch_check(self._p, ctypes.byref(e), _stream(stream))
+        if st not in (HX_OK, HX_ERR_TIMEOUT, HX_ERR_CAPACITY):
+            _check(st, "hx_batch_check")
+        return e.value
 
 
 def set_l2_fetch_granularity(nbytes: int) -> None:

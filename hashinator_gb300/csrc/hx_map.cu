@@ -11,6 +11,7 @@
 #include <cstring>
 #include <mutex>
 #include "hx_host.h"
+#include "hx_internal.h"
 #include "hx_probe.cuh"
 #include "hx_scan.cuh"
 
@@ -260,47 +261,47 @@ __global__ void __launch_bounds__(256) k_insert_t1(const typename PairTraits<P>:
           fail = true;
         }
       }
-      continue;
-    }
-    K ek[U];
-    V ev[U];
-    bool ok[U];
+    } else {
+      K ek[U];
+      V ev[U];
+      bool ok[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      if (act[u]) {
-        h[u] = home_slot(key[u], sp);
-        ok[u] = cas_empty<P>(table + h[u], ek[u], ev[u], key[u], val[u]);
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      if (!act[u]) continue;
-      bool done = ok[u];
-      if (done) {
-        ++ins;
-        maxd = maxd > 1u ? maxd : 1u;
-        continue;
-      }
-      for (int tries = 0; tries < 8 && ek[u] == EMPTY; ++tries) {  // EMPTY with a stale value
-        if (cas_pair(table + h[u], ek[u], ev[u], key[u], val[u])) {
-          ++ins;
-          maxd = maxd > 1u ? maxd : 1u;
-          done = true;
-          break;
+      for (int u = 0; u < U; ++u) {
+        if (act[u]) {
+          h[u] = home_slot(key[u], sp);
+          ok[u] = cas_empty<P>(table + h[u], ek[u], ev[u], key[u], val[u]);
         }
       }
-      if (done) continue;
-      if (ek[u] == key[u]) {
-        store_value(table + h[u], val[u]);
-        continue;
-      }
-      unsigned d1 = 0;
-      const int r = insert_t1_rest<P, B>(table, sp, key[u], val[u], h[u], d1);
-      if (r == PR_INSERTED) {
-        ++ins;
-        maxd = d1 > maxd ? d1 : maxd;
-      } else if (r == PR_FAIL) {
-        fail = true;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (!act[u]) continue;
+        bool done = ok[u];
+        if (done) {
+          ++ins;
+          maxd = maxd > 1u ? maxd : 1u;
+          continue;
+        }
+        for (int tries = 0; tries < 8 && ek[u] == EMPTY; ++tries) {  // EMPTY with a stale value
+          if (cas_pair(table + h[u], ek[u], ev[u], key[u], val[u])) {
+            ++ins;
+            maxd = maxd > 1u ? maxd : 1u;
+            done = true;
+            break;
+          }
+        }
+        if (done) continue;
+        if (ek[u] == key[u]) {
+          store_value(table + h[u], val[u]);
+          continue;
+        }
+        unsigned d1 = 0;
+        const int r = insert_t1_rest<P, B>(table, sp, key[u], val[u], h[u], d1);
+        if (r == PR_INSERTED) {
+          ++ins;
+          maxd = d1 > maxd ? d1 : maxd;
+        } else if (r == PR_FAIL) {
+          fail = true;
+        }
       }
     }
   }
@@ -400,28 +401,7 @@ __global__ void __launch_bounds__(256) k_rehash(const P* __restrict__ old_t, uin
 // host side
 // ---------------------------------------------------------------------------
 
-struct Tuning {
-  int group = 0;   // lanes per key; 0 = automatic policy (auto_policy)
-  int unroll = 1;  // keys in flight per thread when group == 1
-  int block = 256;
-  bool blind = true;  // thread-per-key insert: CAS the home bucket without reading it first
-  bool wide = false;  // thread-per-key windows of 64 B instead of 32 B
-};
-
 }  // namespace hx
-
-struct hx_map {
-  int key_bytes = 0, val_bytes = 0;
-  int sp = 0;
-  int device = 0;
-  void* buckets = nullptr;
-  hx::DInfo* info = nullptr;
-  uint64_t fill_ub = 0;  // host upper bound on fill (exact after a sync)
-  void* scratch = nullptr;
-  uint64_t scratch_bytes = 0;
-  hx::Tuning tune;
-  std::mutex mu;  // guards scratch growth; a map is not thread-safe otherwise
-};
 
 namespace hx {
 
@@ -720,6 +700,21 @@ static hx_status maybe_grow(hx_map* m, uint64_t n, float target_lf, cudaStream_t
 }
 
 static bool valid_map(const hx_map* m) { return m && m->buckets && m->info; }
+
+hx_status map_insert_view(hx_map* m, const void* keys, const void* vals, const void* pairs, uint64_t n,
+                          cudaStream_t s) {
+  m->fill_ub += n;
+  return is_p32(m) ? launch_insert<P32>(m, keys, vals, pairs, n, nullptr, s)
+                   : launch_insert<P64>(m, keys, vals, pairs, n, nullptr, s);
+}
+
+hx_status map_find_view(hx_map* m, const void* keys, void* vals, void* pairs, uint64_t n, bool erase,
+                        cudaStream_t s) {
+  if (erase)
+    return is_p32(m) ? launch_find<P32, true>(m, keys, vals, pairs, n, s) : launch_find<P64, true>(m, keys, vals, pairs, n, s);
+  return is_p32(m) ? launch_find<P32, false>(m, keys, vals, pairs, n, s)
+                   : launch_find<P64, false>(m, keys, vals, pairs, n, s);
+}
 
 }  // namespace hx
 

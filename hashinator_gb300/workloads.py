@@ -89,21 +89,103 @@ def map_workload(n: int, width: int, seed: int, hit_frac: float = 0.5, n_queries
     return keys, vals, np.ascontiguousarray(q), np.ascontiguousarray(erase)
 
 
-def velocity_shell_keys(n: int, centre, r_min: float, r_max: float, rng, grid: int = 200) -> np.ndarray:
-    """n distinct velocity-block IDs id = x + grid*(y + grid*z) on a grid^3
-    mesh, drawn from the shell r_min <= |p - centre| <= r_max."""
-    c = np.asarray(centre, dtype=np.float64)
-    lo = np.maximum(np.floor(c - r_max), 0).astype(np.int64)
-    hi = np.minimum(np.ceil(c + r_max), grid - 1).astype(np.int64)
-    out = np.empty(0, np.uint32)
-    need = n
-    while need > 0:
-        m = max(2 * need, 256)
-        p = rng.integers(lo, hi + 1, size=(m, 3))
-        d = np.sqrt(((p - c) ** 2).sum(axis=1))
-        p = p[(d >= r_min) & (d <= r_max)]
-        ids = (p[:, 0] + grid * (p[:, 1] + grid * p[:, 2])).astype(np.uint32)
-        out = np.unique(np.concatenate([out, ids]))
-        need = n - len(out)
-    rng.shuffle(out)
-    return np.ascontiguousarray(out[:n])
+_SHELL_CACHE: dict = {}
+
+
+def shell_offsets(r_min: float = 30.0, r_max: float = 60.0) -> np.ndarray:
+    """All integer offsets d with r_min <= |d| <= r_max (int16, shape (M, 3))."""
+    key = (r_min, r_max)
+    if key not in _SHELL_CACHE:
+        r = int(np.ceil(r_max))
+        ax = np.arange(-r, r + 1, dtype=np.int32)
+        x, y, z = np.meshgrid(ax, ax, ax, indexing="ij")
+        d2 = x * x + y * y + z * z
+        sel = (d2 >= r_min * r_min) & (d2 <= r_max * r_max)
+        _SHELL_CACHE[key] = np.stack([x[sel], y[sel], z[sel]], axis=1).astype(np.int16)
+    return _SHELL_CACHE[key]
+
+
+def _coprime(rng, mod: np.ndarray) -> np.ndarray:
+    """A random multiplier coprime to each modulus (a bijection j -> a*j mod m)."""
+    import math
+    out = np.empty(len(mod), np.int64)
+    for i, m in enumerate(mod.tolist()):
+        m = max(int(m), 1)
+        while True:
+            a = int(rng.integers(1, max(m, 2)))
+            if math.gcd(a, m) == 1:
+                out[i] = a
+                break
+    return out
+
+
+def _segments(sizes: np.ndarray):
+    """(segment id, index within segment) of every element of a concatenation."""
+    starts = np.zeros(len(sizes), np.int64)
+    starts[1:] = np.cumsum(sizes)[:-1]
+    seg = np.repeat(np.arange(len(sizes)), sizes)
+    j = np.arange(int(sizes.sum()), dtype=np.int64) - starts[seg]
+    return seg, j, starts
+
+
+def batched_workload(n_maps: int, seed: int, log_lo: float = 6.0, log_hi: float = 16.0, hit_frac: float = 0.7,
+                     erase_frac: float = 0.1, grid: int = 200, target_lf: float = 0.5):
+    """Many per-cell velocity-block maps: map i gets n_i = round(2^U), U ~ U[log_lo, log_hi], distinct
+    velocity-block IDs id = x + grid*(y + grid*z) from the 30-60 cell shell around a random centre in
+    [60, 139]^3 (so the shell stays inside the grid), values uniform; size power ceil(log2(n_i / target_lf));
+    n_i queries with hit_frac present keys and the rest absent keys from the same shell, in a shuffled
+    order; a random erase_frac of the keys erased. Distinct draws use random affine permutations
+    j -> (a*j + b) mod M with gcd(a, M) = 1. Returns flat arrays and host offsets."""
+    rng = np.random.default_rng(seed)
+    shell = shell_offsets()
+    m = len(shell)
+    n = np.rint(2.0 ** rng.uniform(log_lo, log_hi, size=n_maps)).astype(np.int64)
+    sp = np.ceil(np.log2(n / target_lf)).astype(np.int32)
+    n_hit = np.rint(n * hit_frac).astype(np.int64)
+    n_miss = n - n_hit
+    n_er = np.rint(n * erase_frac).astype(np.int64)
+    centres = rng.integers(60, 140, size=(n_maps, 3))
+    # keys and misses: distinct shell cells per map
+    need = n + n_miss
+    a = _coprime(rng, np.full(n_maps, m))
+    b = rng.integers(0, m, size=n_maps)
+    seg, j, _ = _segments(need)
+    cell = (a[seg] * j + b[seg]) % m
+    pos = shell[cell].astype(np.int64) + centres[seg]
+    ids = (pos[:, 0] + grid * (pos[:, 1] + grid * pos[:, 2])).astype(np.uint32)
+    is_key = j < n[seg]
+    keys = np.ascontiguousarray(ids[is_key])
+    misses = ids[~is_key]
+    vals = rng.integers(0, 2**32, size=len(keys), dtype=np.uint64).astype(np.uint32)
+    _, _, kstart = _segments(n)
+    _, _, mstart = _segments(n_miss)
+    # queries: n_hit distinct present keys + the misses, shuffled within the map
+    c = _coprime(rng, n)
+    d = rng.integers(0, np.maximum(n, 1))
+    hseg, hj, _ = _segments(n_hit)
+    hits = keys[kstart[hseg] + (c[hseg] * hj + d[hseg]) % n[hseg]]
+    nq = n_hit + n_miss
+    qseg, qj, qstart = _segments(nq)
+    src = np.where(qj < n_hit[qseg], 0, 1)
+    vals_q = np.empty(len(qj), np.uint32)
+    hit_pos = qj < n_hit[qseg]
+    vals_q[hit_pos] = hits
+    vals_q[~hit_pos] = misses
+    del src
+    e_mul = _coprime(rng, nq)
+    f_add = rng.integers(0, np.maximum(nq, 1))
+    queries = np.empty_like(vals_q)
+    queries[qstart[qseg] + (e_mul[qseg] * qj + f_add[qseg]) % nq[qseg]] = vals_q
+    # erase: a distinct erase_frac of each map's keys
+    g = _coprime(rng, n)
+    h = rng.integers(0, np.maximum(n, 1))
+    eseg, ej, _ = _segments(n_er)
+    erase = np.ascontiguousarray(keys[kstart[eseg] + (g[eseg] * ej + h[eseg]) % n[eseg]])
+
+    def offs(sizes):
+        o = np.zeros(n_maps + 1, np.uint64)
+        o[1:] = np.cumsum(sizes)
+        return o
+
+    return {"size_powers": sp, "n": n, "keys": keys, "vals": vals, "ins_offsets": offs(n), "queries": queries,
+            "query_offsets": offs(nq), "erase": erase, "erase_offsets": offs(n_er)}

@@ -223,6 +223,59 @@ hx_status hx_copy_if(const void* d_in, void* d_out, uint64_t n, int elem_bytes, 
                      uint64_t capacity, uint64_t* d_count, uint64_t* h_count, void* d_scratch,
                      uint64_t scratch_bytes, hx_stream stream);
 
+/* ---- batched maps ------------------------------------------------------- */
+/* No reference counterpart as one call: the reference serves many small maps
+ * with one Hashmap object and one launch sequence per map (its per-map
+ * accelerated API above). A batch is a directory of n_maps independent maps
+ * (table i has 2^size_powers[i] buckets, 2 <= size power <= 31) in one device
+ * arena; a plan describes one round of work per map and runs it in a single
+ * persistent launch whose per-map results equal the plain per-map calls. */
+typedef struct hx_batch hx_batch;
+typedef struct hx_batch_plan hx_batch_plan;
+
+/* One round of work. Keys/values/outputs are device arrays; the offsets are
+ * HOST arrays of n_maps + 1 entries (map i owns [off[i], off[i+1])). Any
+ * section may be absent (NULL offsets). Order per map: insert (no growth),
+ * retrieve, erase, then clean_tombstones if clean != 0. */
+typedef struct hx_batch_work {
+  const void* ins_keys;
+  const void* ins_vals;
+  const uint64_t* ins_offsets;
+  const void* query_keys;
+  void* query_out;
+  const uint64_t* query_offsets;
+  const void* erase_keys;
+  const uint64_t* erase_offsets;
+  int clean;
+} hx_batch_work;
+
+hx_status hx_batch_create(hx_batch** out, uint32_t n_maps, const int32_t* size_powers, int key_bytes,
+                          int val_bytes, hx_stream stream);
+hx_status hx_batch_destroy(hx_batch* batch);
+/* clear(targets::device) for every map. */
+hx_status hx_batch_clear(hx_batch* batch, hx_stream stream);
+/* Metadata of one map (synchronises), as hx_get_info. */
+hx_status hx_batch_map_info(hx_batch* batch, uint32_t map, hx_info* out, hx_stream stream);
+hx_status hx_batch_bucket_data(hx_batch* batch, uint32_t map, void** d_buckets, uint64_t* bucket_count);
+
+/* Builds the tile list (synchronises once). The plan keeps the pointers of
+ * `work`; run it as many times as needed. */
+hx_status hx_batch_plan_create(hx_batch* batch, const hx_batch_work* work, hx_batch_plan** out, hx_stream stream);
+hx_status hx_batch_plan_destroy(hx_batch_plan* plan);
+/* group_width in {1,4,8,16,32} lanes per key, block_size in {128,256,512},
+ * tile_keys keys per tile (64..2^20); 0 keeps the current value. */
+hx_status hx_batch_set_tuning(hx_batch_plan* plan, int group_width, int block_size, int tile_keys, hx_stream stream);
+/* The fused persistent launch. */
+hx_status hx_batch_run(hx_batch_plan* plan, hx_stream stream);
+/* The same launch, captured once into a CUDA graph and replayed. */
+hx_status hx_batch_run_graph(hx_batch_plan* plan, hx_stream stream);
+/* The plain path: the per-map launches of hx_insert, hx_retrieve, hx_erase
+ * and hx_clean_tombstones for every map in turn. */
+hx_status hx_batch_run_per_map(hx_batch_plan* plan, hx_stream stream);
+/* Error word of the last fused run (synchronises): 0 ok, 1 a bounded wait ran
+ * out (HX_ERR_TIMEOUT), 2 a moved list overflowed (HX_ERR_CAPACITY). */
+hx_status hx_batch_check(hx_batch_plan* plan, int32_t* error, hx_stream stream);
+
 /* Exclusive u32 scan that allocates nothing. No counterpart in the
  * reference: it is hx_exclusive_scan_u32 for callers that may not allocate
  * device memory when they scan (a host framework that owns all device memory,
