@@ -150,13 +150,75 @@ def cpu_baseline(width: int = 4, log_n: int = 24):
             "seconds": round(total, 3)}
 
 
+def run_batched(args, stream, dev):
+    """4096 velocity-block maps (key counts log-uniform in [2^6, 2^16], LF 0.5): insert all, query (70% hit),
+    erase 10%, clean_tombstones. Fused: one persistent launch, autotuned, replayed from a CUDA graph. Plain:
+    the per-map launches of the single-map API on the same data. Both start from empty maps every step."""
+    import torch
+    import hashinator_gb300 as hx
+    from hashinator_gb300 import workloads
+    from hashinator_gb300.autotune import autotune_batch
+    t0 = time.perf_counter()
+    w = workloads.batched_workload(args.batched_maps, 4096)
+    gen_s = time.perf_counter() - t0
+
+    def dev_u32(a):
+        return torch.from_numpy(a.view(np.int32)).to(dev)
+
+    d = {k: dev_u32(w[k]) for k in ("keys", "vals", "queries", "erase")}
+    outs, batches, plans = [], [], []
+    for _ in range(2):
+        b = hx.Batch(w["size_powers"], stream=stream)
+        o = torch.full((len(w["queries"]),), -1, dtype=torch.int32, device=dev)
+        pl = b.plan(d["keys"], d["vals"], w["ins_offsets"], d["queries"], o, w["query_offsets"], d["erase"],
+                    w["erase_offsets"], clean=True, stream=stream)
+        batches.append(b)
+        plans.append(pl)
+        outs.append(o)
+    bf, bp = batches
+    pf, pp = plans
+    tune = autotune_batch(pf, lambda: bf.clear(stream=stream), stream=stream)
+
+    def timed(fn, reps):
+        ts = []
+        for r in range(reps + 1):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if r:
+                ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    fused_ms = timed(lambda: (bf.clear(stream=stream), pf.run_graph(stream=stream)), max(3, args.steps // 5))
+    plain_ms = timed(lambda: (bp.clear(stream=stream), pp.run_per_map(stream=stream)), 3)
+    err = pf.check(stream=stream)
+    same_q = bool(torch.equal(outs[0], outs[1]))
+    fills_equal = all(bf.map_info(i).fill == bp.map_info(i).fill and
+                      bf.map_info(i).tombstone_counter == bp.map_info(i).tombstone_counter
+                      for i in range(0, bf.n_maps, max(1, bf.n_maps // 256)))
+    n_ops = len(w["keys"]) + len(w["queries"]) + len(w["erase"])
+    return {"workload": f"{args.batched_maps} u32 maps, keys log-uniform in [2^6, 2^16] (velocity-block ids in a "
+                        f"30-60 cell shell of a 200^3 grid), LF 0.5: insert all, query n_i (70% hit), erase 10%, "
+                        f"clean_tombstones",
+            "keys_inserted": int(len(w["keys"])), "queries": int(len(w["queries"])), "erased": int(len(w["erase"])),
+            "buckets": int((2 ** w["size_powers"].astype(np.int64)).sum()),
+            "fused_ms": round(fused_ms, 3), "plain_ms": round(plain_ms, 3),
+            "speedup_vs_per_map": round(plain_ms / fused_ms, 2),
+            "fused_Mops_s": round(n_ops / fused_ms / 1e3, 1), "plain_Mops_s": round(n_ops / plain_ms / 1e3, 1),
+            "autotuned": {"group_width": tune["best"][0], "block": tune["best"][1], "tile_keys": tune["best"][2]},
+            "bit_exact_vs_per_map": same_q and fills_equal and err == 0, "generate_s": round(gen_s, 1),
+            "timing": "CUDA events around clear + run, median; fused replays a captured CUDA graph"}
+
+
 def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
         return 0
     import oracle  # the reference's CPU path, restated (no build of the reference exists on this machine)
     from hashinator_gb300 import workloads
-    log_n = 22
+    log_n = 24
     n = 1 << log_n
     keys, vals, q, _ = workloads.map_workload(n, 4, 1234, erase_frac=0.0)
     out = np.zeros(len(q), keys.dtype)
@@ -374,6 +436,9 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline()
+    batched = None
+    if not args.no_batched:
+        batched = run_batched(args, stream, dev)
 
     if rank == 0:
         metric = METRIC if args.log_keys == 26 else METRIC.replace("2^26 keys, 2^27", f"2^{args.log_keys} keys, 2^{sp}")
@@ -387,6 +452,7 @@ def run_ours(args):
                            "l2": "inputs larger than L2 (1 GiB table, 256 MiB arrays); no flush",
                            "group_width": args.group or "default"},
                 "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+                "batched": batched,
                 "clocks": clocks}
         print(json.dumps(line), flush=True)
     m.close()
@@ -405,6 +471,8 @@ def main():
     ap.add_argument("--log-keys", type=int, default=26, help="log2 of the key count (table: twice as many buckets)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-chunks", type=int, default=8)
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-maps", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -153,6 +153,8 @@ __global__ void __launch_bounds__(BLOCK) k_batch(BatchArgs<P> a) {
       DInfo* inf = a.info + map;
       unsigned ins = 0, maxd = 0, erased = 0, moved = 0;
       bool fail = false;
+      // a group window larger than this table: the thread-per-key path
+      const bool groups = G > 1 && (1ull << sp) >= (unsigned long long)(G * BG);
       switch (t.phase) {
         case BP_INSERT:
         case BP_CLEAN_REINSERT: {
@@ -165,7 +167,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch(BatchArgs<P> a) {
             count = begin < nm ? (nm - begin < count ? nm - begin : count) : 0;
             src = a.moved + a.moved_off[map];
           }
-          if constexpr (G == 1) {
+          if (!groups) {
             for (unsigned k = threadIdx.x; k < count; k += BLOCK) {
               K key;
               V val;
@@ -179,7 +181,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch(BatchArgs<P> a) {
               }
               batch_insert_t1<P, BT>(tab, sp, key, val, ins, maxd, fail);
             }
-          } else {
+          } else if constexpr (G > 1) {
             const unsigned gmask = group_mask<G>(lane);
             for (unsigned k = threadIdx.x / G; k < count; k += BLOCK / G) {
               K key;
@@ -210,7 +212,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch(BatchArgs<P> a) {
           const K* keys = erase ? a.e_keys : a.q_keys;
           const unsigned limit = inf->max_probe;
           if (limit == 0) break;
-          if constexpr (G == 1) {
+          if (!groups) {
             for (unsigned base = 0; base < t.count; base += BLOCK * U) {
               K key[U];
               bool act[U];
@@ -243,7 +245,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch(BatchArgs<P> a) {
                 }
               }
             }
-          } else {
+          } else if constexpr (G > 1) {
             const unsigned gmask = group_mask<G>(lane);
             for (unsigned k = threadIdx.x / G; k < t.count; k += BLOCK / G) {
               const K key = keys[t.begin + k];
