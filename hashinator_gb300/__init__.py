@@ -123,6 +123,7 @@ _SIGS.update({
     "hx_batch_run_graph": [ctypes.c_void_p, ctypes.c_void_p],
     "hx_batch_run_per_map": [ctypes.c_void_p, ctypes.c_void_p],
     "hx_batch_check": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p],
+    "hx_batch_inject_stall": [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
 })
 _EXTRA_SIGS = {
     "hx_status_string": ([ctypes.c_int], ctypes.c_char_p),
@@ -491,6 +492,11 @@ class BatchPlan:
 
     def run_per_map(self, stream=None) -> None:
         _check(self._h.hx_batch_run_per_map(self._p, _stream(stream)), "hx_batch_run_per_map")
+
+    def inject_stall(self, map_index: int, phase: int, enable: bool = True, stream=None) -> None:
+        """Test hook: make the later phases of one map wait for a tile that never runs."""
+        _check(self._h.hx_batch_inject_stall(self._p, map_index, phase, 1 if enable else 0, _stream(stream)),
+               "hx_batch_inject_stall")
 
     def check(self, stream=None) -> int:
         e = ctypes.c_int32()

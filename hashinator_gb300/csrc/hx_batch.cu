@@ -66,7 +66,8 @@ struct BatchArgs {
   const unsigned long long* moved_cap;  // region size per map
 };
 
-constexpr unsigned kBatchSpinLimit = 1u << 22;  // x up to 256 ns: about one second
+constexpr unsigned long long kBatchWaitNs = 1000000000ull;  // one second of global time
+constexpr unsigned kBatchSpinLimit = 1u << 26;                // backstop on the number of polls
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   unsigned v;
@@ -74,10 +75,20 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   return v;
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits until *p == 0, for about one second at most.
 __device__ __forceinline__ bool wait_zero(const unsigned* p) {
+  if (ld_acquire_u32(p) == 0) return true;
+  const unsigned long long t0 = global_ns();
   for (unsigned i = 0; i < kBatchSpinLimit; ++i) {
-    if (ld_acquire_u32(p) == 0) return true;
     __nanosleep(i < 32 ? 32 : 256);
+    if (ld_acquire_u32(p) == 0) return true;
+    if ((i & 63) == 63 && global_ns() - t0 > kBatchWaitNs) return false;
   }
   return false;
 }
@@ -401,6 +412,7 @@ struct hx_batch_plan {
   std::vector<unsigned long long> moved_cap;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
+  std::vector<unsigned> rem_host;  // initial tiles per (phase, map)
 };
 
 namespace hx {
@@ -475,6 +487,7 @@ static hx_status build_tiles(hx_batch_plan* p, cudaStream_t s) {
     HX_CUDA(cudaMemcpyAsync(p->d_tiles, tiles.data(), tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice, s));
   HX_CUDA(cudaMemcpyAsync(p->d_remaining_init, rem.data(), rem.size() * sizeof(unsigned), cudaMemcpyHostToDevice, s));
   HX_CUDA(cudaStreamSynchronize(s));
+  p->rem_host = rem;
   return HX_OK;
 }
 
@@ -808,6 +821,16 @@ hx_status hx_batch_run_per_map(hx_batch_plan* p, hx_stream stream) {
     b->scratch = v.scratch;  // the views share one clean scratch buffer
     b->scratch_bytes = v.scratch_bytes;
   }
+  return HX_OK;
+}
+
+hx_status hx_batch_inject_stall(hx_batch_plan* p, uint32_t map, int phase, int enable, hx_stream stream) {
+  if (!p || map >= p->b->n_maps || phase < 0 || phase >= (int)BP_NPHASES) return HX_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t at = (size_t)phase * p->b->n_maps + map;
+  const unsigned v = p->rem_host[at] + (enable ? 1u : 0u);  // one tile more than will ever run
+  HX_CUDA(cudaMemcpyAsync(p->d_remaining_init + at, &v, sizeof(v), cudaMemcpyHostToDevice, s));
+  HX_CUDA(cudaStreamSynchronize(s));
   return HX_OK;
 }
 

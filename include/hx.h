@@ -275,6 +275,13 @@ hx_status hx_batch_run_per_map(hx_batch_plan* plan, hx_stream stream);
 /* Error word of the last fused run (synchronises): 0 ok, 1 a bounded wait ran
  * out (HX_ERR_TIMEOUT), 2 a moved list overflowed (HX_ERR_CAPACITY). */
 hx_status hx_batch_check(hx_batch_plan* plan, int32_t* error, hx_stream stream);
+/* Failure-detection test hook (no reference counterpart): with enable != 0
+ * the plan's counter of `phase` tiles for `map` starts one higher than the
+ * tiles that exist, so every later-phase tile of that map waits in vain
+ * until its bounded wait (about one second) runs out; the launch still
+ * returns and hx_batch_check reports HX_ERR_TIMEOUT. enable = 0 undoes it.
+ * Phases: 0 insert, 1 query, 2 erase, 3..5 clean_tombstones. Synchronises. */
+hx_status hx_batch_inject_stall(hx_batch_plan* plan, uint32_t map, int phase, int enable, hx_stream stream);
 
 /* Exclusive u32 scan that allocates nothing. No counterpart in the
  * reference: it is hx_exclusive_scan_u32 for callers that may not allocate

@@ -143,3 +143,29 @@ def test_autotune_keeps_results_exact(hx, oracle_mod):
     p.run()
     torch.cuda.synchronize()
     _check_against(b, out, w, ref)
+
+
+def test_bounded_wait_reports_timeout_and_context_survives(hx, oracle_mod):
+    """Failure detection without a GPU fault: one map's insert phase is never
+    counted off (a flag nothing sets), its later tiles' bounded waits run out,
+    the launch returns, the error word says timeout, and the next clean run on
+    the same context is exact."""
+    import time
+    import torch
+    w = _work(n_maps=6, seed=21, lo=6.0, hi=7.0)  # one tile per phase per map
+    ref = _oracle(oracle_mod, w)
+    b = hx.Batch(w["size_powers"])
+    p, out, _ = _plan(hx, b, w, "cuda")
+    p.inject_stall(0, 0)  # phase 0 (insert) of map 0
+    t0 = time.time()
+    p.run()
+    torch.cuda.synchronize()
+    assert p.check() == 1  # a bounded wait ran out
+    assert time.time() - t0 < 30
+    p.inject_stall(0, 0, enable=False)
+    b.clear()
+    out.fill_(int(np.int32(np.uint32(FILL).view(np.int32))))
+    p.run()
+    torch.cuda.synchronize()
+    assert p.check() == 0
+    _check_against(b, out, w, ref)
