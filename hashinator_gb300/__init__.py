@@ -24,8 +24,8 @@ import ctypes
 import os
 from pathlib import Path
 
-__all__ = ["lib", "HXError", "Hashmap", "Pred", "tools", "Batch", "BatchPlan", "STATUS_SUCCESS", "STATUS_FAIL",
-           "STATUS_INVALID", "LIB_PATH", "Info"]
+__all__ = ["lib", "HXError", "Hashmap", "Pred", "tools", "Batch", "BatchPlan", "Server", "Request", "Completion",
+           "STATUS_SUCCESS", "STATUS_FAIL", "STATUS_INVALID", "LIB_PATH", "Info"]
 
 LIB_PATH = Path(__file__).resolve().parent / "libhx.so"
 
@@ -77,6 +77,20 @@ class _CBatchWork(ctypes.Structure):
                 ("clean", ctypes.c_int)]
 
 
+class Request(ctypes.Structure):
+    """hx_request."""
+    _fields_ = [("map", ctypes.c_uint32), ("op", ctypes.c_uint32), ("keys", ctypes.c_void_p),
+                ("vals", ctypes.c_void_p), ("out", ctypes.c_void_p), ("n", ctypes.c_uint64), ("tag", ctypes.c_uint64)]
+
+
+class Completion(ctypes.Structure):
+    """hx_completion."""
+    _fields_ = [("tag", ctypes.c_uint64), ("complete_ns", ctypes.c_uint64), ("status", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+OP_INSERT, OP_QUERY, OP_ERASE = 0, 1, 2
+
 _lib_handle = None
 
 _SIGS = {
@@ -124,6 +138,22 @@ _SIGS.update({
     "hx_batch_run_per_map": [ctypes.c_void_p, ctypes.c_void_p],
     "hx_batch_check": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p],
     "hx_batch_inject_stall": [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
+})
+_SIGS.update({
+    "hx_server_create": [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_uint64, ctypes.c_float,
+                         ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32],
+    "hx_server_destroy": [ctypes.c_void_p],
+    "hx_server_add_map": [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32)],
+    "hx_server_submit": [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_uint32],
+    "hx_server_step": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32)],
+    "hx_server_poll": [ctypes.c_void_p, ctypes.POINTER(Completion), ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)],
+    "hx_server_drain": [ctypes.c_void_p],
+    "hx_server_map_info": [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(Info)],
+    "hx_server_bucket_data": [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p),
+                              ctypes.POINTER(ctypes.c_uint64)],
+    "hx_server_memory": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)],
+    "hx_server_run_trace": [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_void_p, ctypes.c_uint32,
+                            ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)],
 })
 _EXTRA_SIGS = {
     "hx_status_string": ([ctypes.c_int], ctypes.c_char_p),
@@ -504,6 +534,92 @@ class BatchPlan:
         if st not in (HX_OK, HX_ERR_TIMEOUT, HX_ERR_CAPACITY):
             _check(st, "hx_batch_check")
         return e.value
+
+
+class Server:
+    """Serving loop over many resident maps (hx_server)."""
+
+    def __init__(self, key_bytes: int = 8, memory_budget: int = 40 << 30, max_load_factor: float = 0.8,
+                 max_maps: int = 4096, max_round_requests: int = 4096, max_round_keys: int = 1 << 24,
+                 rounds_in_flight: int = 3):
+        self._h = lib()
+        self.key_bytes = key_bytes
+        self._s = ctypes.c_void_p()
+        _check(self._h.hx_server_create(ctypes.byref(self._s), key_bytes, memory_budget, max_load_factor, max_maps,
+                                        max_round_requests, max_round_keys, rounds_in_flight), "hx_server_create")
+
+    def close(self) -> None:
+        if self._s and self._s.value:
+            _check(self._h.hx_server_destroy(self._s), "hx_server_destroy")
+            self._s = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_map(self, size_power: int) -> int:
+        mid = ctypes.c_uint32()
+        _check(self._h.hx_server_add_map(self._s, size_power, ctypes.byref(mid)), "hx_server_add_map")
+        return mid.value
+
+    def try_add_map(self, size_power: int):
+        mid = ctypes.c_uint32()
+        st = self._h.hx_server_add_map(self._s, size_power, ctypes.byref(mid))
+        return mid.value if st == HX_OK else None
+
+    @staticmethod
+    def requests(reqs) -> "ctypes.Array":
+        arr = (Request * len(reqs))()
+        for i, r in enumerate(reqs):
+            arr[i] = r if isinstance(r, Request) else Request(*r)
+        return arr
+
+    def submit(self, reqs) -> None:
+        arr = reqs if isinstance(reqs, ctypes.Array) else self.requests(reqs)
+        _check(self._h.hx_server_submit(self._s, arr, len(arr)), "hx_server_submit")
+
+    def step(self) -> int:
+        n = ctypes.c_uint32()
+        _check(self._h.hx_server_step(self._s, ctypes.byref(n)), "hx_server_step")
+        return n.value
+
+    def poll(self, capacity: int = 65536) -> list:
+        buf = (Completion * capacity)()
+        n = ctypes.c_uint32()
+        _check(self._h.hx_server_poll(self._s, buf, capacity, ctypes.byref(n)), "hx_server_poll")
+        return [(buf[i].tag, buf[i].complete_ns, buf[i].status) for i in range(n.value)]
+
+    def drain(self) -> None:
+        _check(self._h.hx_server_drain(self._s), "hx_server_drain")
+
+    def map_info(self, i: int) -> Info:
+        inf = Info()
+        _check(self._h.hx_server_map_info(self._s, i, ctypes.byref(inf)), "hx_server_map_info")
+        return inf
+
+    def bucket_data(self, i: int) -> tuple[int, int]:
+        p, n = ctypes.c_void_p(), ctypes.c_uint64()
+        _check(self._h.hx_server_bucket_data(self._s, i, ctypes.byref(p), ctypes.byref(n)), "hx_server_bucket_data")
+        return p.value, n.value
+
+    def memory(self) -> tuple[int, int]:
+        u, b = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(self._h.hx_server_memory(self._s, ctypes.byref(u), ctypes.byref(b)), "hx_server_memory")
+        return u.value, b.value
+
+    def run_trace(self, reqs, arrival_ns):
+        """Real-time replay; returns (complete_ns, status) numpy arrays."""
+        import numpy as _np
+        arr = reqs if isinstance(reqs, ctypes.Array) else self.requests(reqs)
+        arrival = _np.ascontiguousarray(arrival_ns, dtype=_np.uint64)
+        comp = _np.zeros(len(arr), _np.uint64)
+        st = _np.zeros(len(arr), _np.int32)
+        t0 = ctypes.c_uint64()
+        _check(self._h.hx_server_run_trace(self._s, arr, arrival.ctypes.data, len(arr), comp.ctypes.data,
+                                           st.ctypes.data, ctypes.byref(t0)), "hx_server_run_trace")
+        return comp, st
 
 
 def set_l2_fetch_granularity(nbytes: int) -> None:

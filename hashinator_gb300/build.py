@@ -21,7 +21,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libhx.so"
 
-CUDA_SOURCES = ["hx_map.cu", "hx_scan.cu", "hx_batch.cu", "hx_noalloc.cu"]
+CUDA_SOURCES = ["hx_map.cu", "hx_scan.cu", "hx_batch.cu", "hx_serve.cu", "hx_noalloc.cu"]
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-lineinfo", "-O3", "-std=c++17",

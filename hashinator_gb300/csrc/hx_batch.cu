@@ -93,39 +93,6 @@ __device__ __forceinline__ bool wait_zero(const unsigned* p) {
   return false;
 }
 
-// One key into one table, thread-per-key: blind CAS at home, then probe.
-template <class P, int B>
-__device__ __forceinline__ void batch_insert_t1(P* tab, int sp, typename PairTraits<P>::K key,
-                                                typename PairTraits<P>::V val, unsigned& ins, unsigned& maxd,
-                                                bool& fail) {
-  using K = typename PairTraits<P>::K;
-  using V = typename PairTraits<P>::V;
-  if (key == PairTraits<P>::EMPTY || key == PairTraits<P>::TOMB) return;
-  const uint32_t h = home_slot(key, sp);
-  K ek = PairTraits<P>::EMPTY;
-  V ev = 0;
-  for (int tries = 0; tries < 9; ++tries) {
-    if (cas_pair(tab + h, ek, ev, key, val)) {
-      ++ins;
-      maxd = maxd > 1u ? maxd : 1u;
-      return;
-    }
-    if (ek != PairTraits<P>::EMPTY) break;  // taken (or EMPTY with a stale value: retry)
-  }
-  if (ek == key) {
-    store_value(tab + h, val);
-    return;
-  }
-  unsigned d1 = 0;
-  const int r = insert_t1_rest<P, B>(tab, sp, key, val, h, d1);
-  if (r == PR_INSERTED) {
-    ++ins;
-    maxd = d1 > maxd ? d1 : maxd;
-  } else if (r == PR_FAIL) {
-    fail = true;
-  }
-}
-
 template <class P, int G, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_batch(BatchArgs<P> a) {
   using K = typename PairTraits<P>::K;
@@ -190,7 +157,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch(BatchArgs<P> a) {
                 key = a.ins_keys[begin + k];
                 val = a.ins_vals[begin + k];
               }
-              batch_insert_t1<P, BT>(tab, sp, key, val, ins, maxd, fail);
+              insert_one_t1<P, BT>(tab, sp, key, val, ins, maxd, fail);
             }
           } else if constexpr (G > 1) {
             const unsigned gmask = group_mask<G>(lane);

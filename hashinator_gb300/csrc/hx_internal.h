@@ -40,4 +40,7 @@ hx_status map_insert_view(hx_map* m, const void* keys, const void* vals, const v
                           cudaStream_t s);
 hx_status map_find_view(hx_map* m, const void* keys, void* vals, void* pairs, uint64_t n, bool erase,
                         cudaStream_t s);
+// device_rehash of the viewed table into a new cudaMallocAsync allocation of
+// 2^new_sp buckets; the old bucket array is released stream-ordered.
+hx_status map_rehash_view(hx_map* m, int new_sp, cudaStream_t s);
 }  // namespace hx

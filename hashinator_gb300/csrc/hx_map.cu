@@ -701,6 +701,8 @@ static hx_status maybe_grow(hx_map* m, uint64_t n, float target_lf, cudaStream_t
 
 static bool valid_map(const hx_map* m) { return m && m->buckets && m->info; }
 
+hx_status map_rehash_view(hx_map* m, int new_sp, cudaStream_t s) { return rehash(m, new_sp, s); }
+
 hx_status map_insert_view(hx_map* m, const void* keys, const void* vals, const void* pairs, uint64_t n,
                           cudaStream_t s) {
   m->fill_ub += n;

@@ -333,4 +333,37 @@ __device__ __forceinline__ int insert_t1_win(P* __restrict__ table, int sp, type
   }
 }
 
+// One key into one table, thread-per-key: blind CAS at home, then probe.
+template <class P, int B>
+__device__ __forceinline__ void insert_one_t1(P* tab, int sp, typename PairTraits<P>::K key,
+                                                typename PairTraits<P>::V val, unsigned& ins, unsigned& maxd,
+                                                bool& fail) {
+  using K = typename PairTraits<P>::K;
+  using V = typename PairTraits<P>::V;
+  if (key == PairTraits<P>::EMPTY || key == PairTraits<P>::TOMB) return;
+  const uint32_t h = home_slot(key, sp);
+  K ek = PairTraits<P>::EMPTY;
+  V ev = 0;
+  for (int tries = 0; tries < 9; ++tries) {
+    if (cas_pair(tab + h, ek, ev, key, val)) {
+      ++ins;
+      maxd = maxd > 1u ? maxd : 1u;
+      return;
+    }
+    if (ek != PairTraits<P>::EMPTY) break;  // taken (or EMPTY with a stale value: retry)
+  }
+  if (ek == key) {
+    store_value(tab + h, val);
+    return;
+  }
+  unsigned d1 = 0;
+  const int r = insert_t1_rest<P, B>(tab, sp, key, val, h, d1);
+  if (r == PR_INSERTED) {
+    ++ins;
+    maxd = d1 > maxd ? d1 : maxd;
+  } else if (r == PR_FAIL) {
+    fail = true;
+  }
+}
+
 }  // namespace hx

@@ -1,0 +1,636 @@
+// hx_serve.cu — serving loop: continuous batching of insert / query / erase
+// requests over many resident maps.
+//
+// Requests are queued as they arrive. A step takes the requests at the head
+// of the queue (up to a key and request budget) and runs them as one round:
+// one fused persistent launch in which requests on different maps proceed
+// concurrently, while requests on the same map are chained in admission
+// order (a request's tiles wait, bounded, until its predecessor on that map
+// is done — the same ticket argument as the batched kernel: predecessors are
+// earlier in the ticket order, so only running CTAs are ever waited on).
+// Several rounds are in flight at once: the host forms round k+1 while the
+// GPU runs round k, and requests that arrive meanwhile join the next round.
+//
+// Every table stays resident. Before a round, a map whose load factor would
+// pass the limit after the round's inserts is grown by an on-device rehash
+// (device_rehash, hashinator.h:285-336) into a table allocated against the
+// server's device-memory budget; an insert that cannot be admitted within the
+// budget is rejected and reported, the map's other requests proceed.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <vector>
+
+#include "hx_host.h"
+#include "hx_internal.h"
+#include "hx_probe.cuh"
+
+namespace hx {
+
+enum : unsigned { SOP_INSERT = 0, SOP_QUERY = 1, SOP_ERASE = 2 };
+
+struct SReq {
+  const void* keys;
+  const void* vals;
+  void* out;
+  unsigned long long n;
+  unsigned map;
+  unsigned op;
+  int prev;  // previous request on the same map in this round, or -1
+  unsigned pad;
+};
+struct STile {
+  unsigned req;
+  unsigned count;
+  unsigned long long begin;
+};
+struct SMap {
+  void* table;
+  int sp;
+  int pad;
+};
+
+template <class P>
+struct ServeArgs {
+  const SMap* maps;
+  DInfo* info;
+  const SReq* reqs;
+  const STile* tiles;
+  unsigned n_tiles;
+  unsigned* work;
+  unsigned* error;
+  unsigned* remaining;  // tiles left per request
+};
+
+constexpr unsigned long long kServeWaitNs = 1000000000ull;
+
+__device__ __forceinline__ bool serve_wait_zero(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  if (v == 0) return true;
+  unsigned long long t0, t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (unsigned i = 0; i < (1u << 26); ++i) {
+    __nanosleep(i < 32 ? 32 : 256);
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    if (v == 0) return true;
+    if ((i & 63) == 63) {
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+      if (t - t0 > kServeWaitNs) return false;
+    }
+  }
+  return false;
+}
+
+template <class P>
+__global__ void __launch_bounds__(256) k_serve(ServeArgs<P> a) {
+  using K = typename PairTraits<P>::K;
+  using V = typename PairTraits<P>::V;
+  constexpr int BLOCK = 256;
+  constexpr int BT = sizeof(P) == 8 ? 4 : 2;
+  constexpr int U = 2;
+  __shared__ STile s_t;
+  __shared__ SReq s_r;
+  __shared__ unsigned s_ok, s_ins, s_max, s_fail, s_erased, s_end;
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const unsigned idx = atomicAdd(a.work, 1u);
+      s_end = idx >= a.n_tiles;
+      s_ins = s_max = s_fail = s_erased = 0;
+      s_ok = 1;
+      if (!s_end) {
+        s_t = a.tiles[idx];
+        s_r = a.reqs[s_t.req];
+        if (s_r.prev >= 0 && !serve_wait_zero(a.remaining + s_r.prev)) {
+          s_ok = 0;
+          atomicExch(a.error, 1u);
+        }
+      }
+    }
+    __syncthreads();
+    if (s_end) break;
+    __threadfence();
+    const STile t = s_t;
+    const SReq r = s_r;
+    if (s_ok) {
+      const SMap md = a.maps[r.map];
+      P* tab = static_cast<P*>(md.table);
+      const int sp = md.sp;
+      DInfo* inf = a.info + r.map;
+      unsigned ins = 0, maxd = 0, erased = 0;
+      bool fail = false;
+      const K* keys = static_cast<const K*>(r.keys);
+      if (r.op == SOP_INSERT) {
+        const V* vals = static_cast<const V*>(r.vals);
+        for (unsigned k = threadIdx.x; k < t.count; k += BLOCK)
+          insert_one_t1<P, BT>(tab, sp, keys[t.begin + k], vals[t.begin + k], ins, maxd, fail);
+      } else {
+        const bool erase = r.op == SOP_ERASE;
+        V* out = static_cast<V*>(r.out);
+        const unsigned limit = inf->max_probe;
+        if (limit) {
+          for (unsigned base = 0; base < t.count; base += BLOCK * U) {
+            K key[U];
+            bool act[U];
+            uint32_t h[U];
+            Window<P, BT> w[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              const unsigned k = base + u * BLOCK + threadIdx.x;
+              act[u] = k < t.count;
+              if (act[u]) {
+                key[u] = keys[t.begin + k];
+                act[u] = key[u] != PairTraits<P>::EMPTY && key[u] != PairTraits<P>::TOMB;
+              }
+              if (act[u]) {
+                h[u] = home_slot(key[u], sp);
+                load_buckets<BT>(tab + (h[u] & ~(uint32_t)(BT - 1)), w[u].k, w[u].v);
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              if (!act[u]) continue;
+              uint32_t slot;
+              V v;
+              if (find_t1<P, BT>(tab, sp, key[u], limit, h[u], w[u], slot, v)) {
+                if (erase) {
+                  if (cas_key(tab + slot, key[u], PairTraits<P>::TOMB)) ++erased;
+                } else {
+                  out[t.begin + base + u * BLOCK + threadIdx.x] = v;
+                }
+              }
+            }
+          }
+        }
+      }
+      ins = __reduce_add_sync(0xffffffffu, ins);
+      maxd = __reduce_max_sync(0xffffffffu, maxd);
+      erased = __reduce_add_sync(0xffffffffu, erased);
+      const bool anyfail = __any_sync(0xffffffffu, fail);
+      if (lane == 0) {
+        if (ins) atomicAdd(&s_ins, ins);
+        if (maxd) atomicMax(&s_max, maxd);
+        if (erased) atomicAdd(&s_erased, erased);
+        if (anyfail) atomicExch(&s_fail, 1u);
+      }
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      DInfo* inf = a.info + r.map;
+      if (s_ins) atomicAdd(&inf->fill, (unsigned long long)s_ins);
+      if (s_max) atomicMax(&inf->max_probe, s_max);
+      if (s_fail) atomicExch(&inf->err, HX_STATUS_FAIL);
+      if (s_erased) {
+        atomicAdd(&inf->tombstones, (unsigned long long)s_erased);
+        atomicAdd(&inf->fill, 0ull - (unsigned long long)s_erased);
+      }
+      __threadfence();
+      atomicSub(a.remaining + t.req, 1u);
+    }
+  }
+}
+
+static uint64_t now_ns() {
+  return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
+             std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+struct ServeMap {
+  int sp = 0;
+  void* table = nullptr;
+  uint64_t bytes = 0;
+  uint64_t fill_ub = 0;    // upper bound of fill once every launched round is done
+  uint64_t in_flight = 0;  // inserts launched in rounds not yet completed
+};
+
+struct Pending {
+  hx_request r;
+  uint64_t seq;
+};
+
+struct Slot {
+  bool busy = false;
+  uint64_t round_no = 0;  // launch order
+  size_t n_maps = 0;      // maps covered by this round's metadata snapshot
+  SReq* h_reqs = nullptr;
+  STile* h_tiles = nullptr;
+  unsigned* h_rem = nullptr;
+  SMap* h_dir = nullptr;
+  DInfo* h_info = nullptr;
+  unsigned* h_err = nullptr;
+  SReq* d_reqs = nullptr;
+  STile* d_tiles = nullptr;
+  unsigned* d_cnt = nullptr;  // work, error, remaining[]
+  cudaEvent_t done = nullptr;
+  std::vector<uint64_t> tags;
+  std::vector<std::pair<unsigned, uint64_t>> inserts;  // (map, keys) launched in this round
+};
+
+}  // namespace hx
+
+struct hx_server {
+  int kb = 8;
+  uint64_t budget = 0, used = 0;
+  float max_lf = 0.8f;
+  uint32_t max_maps = 0;
+  uint32_t max_round_requests = 0;
+  uint64_t max_round_keys = 0;
+  uint32_t tile_keys = 4096;
+  std::vector<hx::ServeMap> maps;
+  hx::SMap* d_maps = nullptr;
+  hx::DInfo* d_info = nullptr;
+  cudaStream_t s = nullptr;
+  std::deque<hx::Pending> queue;
+  std::vector<hx::Slot> slots;
+  uint64_t seq = 0;
+  uint64_t rounds = 0;
+  cudaEvent_t t0 = nullptr;
+  uint64_t t0_ns = 0;
+  bool t0_set = false;
+  std::vector<hx_completion> done;  // completed since the last poll
+  uint64_t timeouts = 0;
+};
+
+namespace hx {
+
+static uint64_t pb(const hx_server* sv) { return sv->kb == 4 ? 8 : 16; }
+
+static void view_of(hx_server* sv, unsigned i, hx_map* v) {
+  v->key_bytes = sv->kb;
+  v->val_bytes = sv->kb;
+  v->sp = sv->maps[i].sp;
+  v->buckets = sv->maps[i].table;
+  v->info = sv->d_info + i;
+  v->fill_ub = sv->maps[i].fill_ub;
+}
+
+// Completed rounds: completion times, fill bounds refreshed from the
+// round's metadata snapshot.
+static hx_status reap(hx_server* sv, bool wait_oldest) {
+  // rounds run in launch order on one stream: reap them in that order
+  std::vector<Slot*> busy;
+  for (auto& sl : sv->slots)
+    if (sl.busy) busy.push_back(&sl);
+  std::sort(busy.begin(), busy.end(), [](const Slot* a, const Slot* b) { return a->round_no < b->round_no; });
+  for (Slot* slp : busy) {
+    Slot& sl = *slp;
+    cudaError_t q = wait_oldest ? cudaEventSynchronize(sl.done) : cudaEventQuery(sl.done);
+    wait_oldest = false;
+    if (q == cudaErrorNotReady) break;
+    if (q != cudaSuccess) return cuda_status(q);
+    float ms = 0.f;
+    if (sv->t0_set) cudaEventElapsedTime(&ms, sv->t0, sl.done);
+    const uint64_t t_ns = sv->t0_ns + (uint64_t)((double)ms * 1e6);
+    const int32_t st = *sl.h_err ? HX_ERR_TIMEOUT : HX_OK;
+    if (*sl.h_err) sv->timeouts++;
+    for (uint64_t tag : sl.tags) sv->done.push_back(hx_completion{tag, t_ns, st, 0});
+    for (auto& ins : sl.inserts) sv->maps[ins.first].in_flight -= ins.second;
+    for (size_t i = 0; i < sl.n_maps && i < sv->maps.size(); ++i)
+      sv->maps[i].fill_ub = sl.h_info[i].fill + sv->maps[i].in_flight;
+    sl.busy = false;
+    sl.tags.clear();
+    sl.inserts.clear();
+  }
+  return HX_OK;
+}
+
+}  // namespace hx
+
+using namespace hx;
+
+extern "C" {
+
+hx_status hx_server_create(hx_server** out, int key_bytes, uint64_t memory_budget_bytes, float max_load_factor,
+                           uint32_t max_maps, uint32_t max_round_requests, uint64_t max_round_keys,
+                           uint32_t rounds_in_flight) {
+  if (!out || (key_bytes != 4 && key_bytes != 8) || !(max_load_factor > 0.f && max_load_factor <= 1.f) ||
+      max_maps == 0 || max_round_requests == 0 || max_round_keys == 0 || rounds_in_flight == 0 ||
+      rounds_in_flight > 16)
+    return HX_ERR_INVALID_ARG;
+  *out = nullptr;
+  hx_server* sv = new hx_server();
+  sv->kb = key_bytes;
+  sv->budget = memory_budget_bytes;
+  sv->max_lf = max_load_factor;
+  sv->max_maps = max_maps;
+  sv->max_round_requests = max_round_requests;
+  sv->max_round_keys = max_round_keys;
+  const uint64_t max_tiles = max_round_requests + max_round_keys / sv->tile_keys + 1;
+  cudaError_t e = cudaStreamCreateWithFlags(&sv->s, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&sv->d_maps), max_maps * sizeof(SMap));
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&sv->d_info), max_maps * sizeof(DInfo));
+  if (e == cudaSuccess) e = cudaEventCreate(&sv->t0);
+  sv->slots.resize(rounds_in_flight);
+  for (auto& sl : sv->slots) {
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&sl.h_reqs), max_round_requests * sizeof(SReq));
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&sl.h_tiles), max_tiles * sizeof(STile));
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&sl.h_rem), max_round_requests * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&sl.h_dir), max_maps * sizeof(SMap));
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&sl.h_info), max_maps * sizeof(DInfo));
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&sl.h_err), sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&sl.d_reqs), max_round_requests * sizeof(SReq));
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&sl.d_tiles), max_tiles * sizeof(STile));
+    if (e == cudaSuccess)
+      e = cudaMalloc(reinterpret_cast<void**>(&sl.d_cnt), (2 + max_round_requests) * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDefault);
+  }
+  if (e != cudaSuccess) {
+    *out = sv;
+    hx_server_destroy(sv);
+    *out = nullptr;
+    return cuda_status(e);
+  }
+  *out = sv;
+  return HX_OK;
+}
+
+hx_status hx_server_destroy(hx_server* sv) {
+  if (!sv) return HX_ERR_INVALID_ARG;
+  if (sv->s) cudaStreamSynchronize(sv->s);
+  for (auto& m : sv->maps) cudaFree(m.table);
+  for (auto& sl : sv->slots) {
+    cudaFreeHost(sl.h_reqs);
+    cudaFreeHost(sl.h_tiles);
+    cudaFreeHost(sl.h_rem);
+    cudaFreeHost(sl.h_dir);
+    cudaFreeHost(sl.h_info);
+    cudaFreeHost(sl.h_err);
+    cudaFree(sl.d_reqs);
+    cudaFree(sl.d_tiles);
+    cudaFree(sl.d_cnt);
+    if (sl.done) cudaEventDestroy(sl.done);
+  }
+  cudaFree(sv->d_maps);
+  cudaFree(sv->d_info);
+  if (sv->t0) cudaEventDestroy(sv->t0);
+  if (sv->s) cudaStreamDestroy(sv->s);
+  delete sv;
+  return HX_OK;
+}
+
+hx_status hx_server_add_map(hx_server* sv, int size_power, uint32_t* map_id) {
+  if (!sv || !map_id || size_power < 2 || size_power > 31) return HX_ERR_INVALID_ARG;
+  if (sv->maps.size() >= sv->max_maps) return HX_ERR_CAPACITY;
+  const uint64_t bytes = (1ull << size_power) * pb(sv);
+  if (sv->used + bytes > sv->budget) return HX_ERR_OOM;  // admission against the budget
+  ServeMap m;
+  m.sp = size_power;
+  m.bytes = bytes;
+  HX_CUDA(cudaMallocAsync(&m.table, bytes, sv->s));
+  hx_map v;
+  v.key_bytes = sv->kb;
+  v.val_bytes = sv->kb;
+  v.sp = size_power;
+  v.buckets = m.table;
+  const uint32_t id = (uint32_t)sv->maps.size();
+  v.info = sv->d_info + id;
+  hx_status st = hx_clear(&v, sv->s);
+  if (st != HX_OK) {
+    cudaFreeAsync(m.table, sv->s);
+    return st;
+  }
+  sv->used += bytes;
+  sv->maps.push_back(m);
+  *map_id = id;
+  return HX_OK;
+}
+
+hx_status hx_server_submit(hx_server* sv, const hx_request* reqs, uint32_t count) {
+  if (!sv || (count && !reqs)) return HX_ERR_INVALID_ARG;
+  for (uint32_t i = 0; i < count; ++i) {
+    const hx_request& r = reqs[i];
+    if (r.map >= sv->maps.size() || r.op > SOP_ERASE || (r.n && !r.keys) || (r.op == SOP_INSERT && r.n && !r.vals) ||
+        (r.op == SOP_QUERY && r.n && !r.out))
+      return HX_ERR_INVALID_ARG;
+  }
+  for (uint32_t i = 0; i < count; ++i) sv->queue.push_back(Pending{reqs[i], sv->seq++});
+  return HX_OK;
+}
+
+hx_status hx_server_step(hx_server* sv, uint32_t* launched) {
+  if (!sv) return HX_ERR_INVALID_ARG;
+  if (launched) *launched = 0;
+  hx_status st = reap(sv, false);
+  if (st != HX_OK) return st;
+  if (sv->queue.empty()) return HX_OK;
+  Slot* sl = nullptr;
+  for (auto& x : sv->slots)
+    if (!x.busy) {
+      sl = &x;
+      break;
+    }
+  if (!sl) return HX_OK;  // every round slot is in flight
+  if (!sv->t0_set) {
+    HX_CUDA(cudaEventRecord(sv->t0, sv->s));
+    sv->t0_ns = now_ns();
+    sv->t0_set = true;
+  }
+  // Take requests from the head of the queue.
+  std::vector<Pending> round;
+  uint64_t keys = 0;
+  while (!sv->queue.empty() && round.size() < sv->max_round_requests) {
+    const Pending& p = sv->queue.front();
+    if (!round.empty() && keys + p.r.n > sv->max_round_keys) break;
+    keys += p.r.n;
+    round.push_back(p);
+    sv->queue.pop_front();
+  }
+  // Growth and admission of inserts, in admission order.
+  std::vector<uint64_t> add(sv->maps.size(), 0);
+  std::vector<char> admitted(round.size(), 1);
+  for (size_t i = 0; i < round.size(); ++i) {
+    const hx_request& r = round[i].r;
+    if (r.op != SOP_INSERT || r.n == 0) continue;
+    ServeMap& m = sv->maps[r.map];
+    const uint64_t proj = m.fill_ub + add[r.map] + r.n;
+    if ((double)proj > (double)sv->max_lf * (double)(1ull << m.sp)) {
+      int nsp = m.sp;
+      while ((double)proj > (double)sv->max_lf * (double)(1ull << nsp) && nsp < 31) ++nsp;
+      const uint64_t nbytes = (1ull << nsp) * pb(sv);
+      if (sv->used - m.bytes + nbytes > sv->budget || (double)proj > (double)sv->max_lf * (double)(1ull << nsp)) {
+        admitted[i] = 0;  // cannot grow within the budget: reject this insert
+        continue;
+      }
+      hx_map v;
+      view_of(sv, r.map, &v);
+      st = map_rehash_view(&v, nsp, sv->s);  // on-device rehash, stream-ordered after earlier rounds
+      if (st != HX_OK) return st;
+      sv->used = sv->used - m.bytes + nbytes;
+      m.table = v.buckets;
+      m.sp = nsp;
+      m.bytes = nbytes;
+    }
+    add[r.map] += r.n;
+  }
+  // Chain requests per map, order tiles by rank within the map.
+  std::vector<int> last(sv->maps.size(), -1), rank_of(sv->maps.size(), 0);
+  std::vector<std::pair<int, unsigned>> order;  // (rank, request index in round)
+  unsigned nreq = 0;
+  sl->tags.clear();
+  sl->inserts.clear();
+  for (size_t i = 0; i < round.size(); ++i) {
+    const hx_request& r = round[i].r;
+    if (!admitted[i]) {
+      sv->done.push_back(hx_completion{r.tag, now_ns(), HX_ERR_OOM, 0});
+      continue;
+    }
+    SReq q;
+    q.keys = r.keys;
+    q.vals = r.vals;
+    q.out = r.out;
+    q.n = r.n;
+    q.map = r.map;
+    q.op = r.op;
+    q.prev = last[r.map];
+    q.pad = 0;
+    last[r.map] = (int)nreq;
+    sl->h_reqs[nreq] = q;
+    order.push_back({rank_of[r.map]++, nreq});
+    sl->tags.push_back(r.tag);
+    if (r.op == SOP_INSERT && r.n) sl->inserts.push_back({r.map, r.n});
+    ++nreq;
+  }
+  if (nreq == 0) return HX_OK;
+  std::stable_sort(order.begin(), order.end(),
+                   [](const std::pair<int, unsigned>& a, const std::pair<int, unsigned>& b) { return a.first < b.first; });
+  unsigned ntiles = 0;
+  for (auto& o : order) {
+    const SReq& q = sl->h_reqs[o.second];
+    unsigned nt = 0;
+    for (uint64_t a0 = 0; a0 < q.n || nt == 0; a0 += sv->tile_keys) {
+      const uint64_t c = q.n > a0 ? std::min<uint64_t>(sv->tile_keys, q.n - a0) : 0;
+      sl->h_tiles[ntiles++] = STile{o.second, (unsigned)c, a0};
+      ++nt;
+      if (q.n == 0) break;
+    }
+    sl->h_rem[o.second] = nt;
+  }
+  for (auto& x : sl->inserts) sv->maps[x.first].in_flight += x.second;
+  for (size_t i = 0; i < sv->maps.size(); ++i) sl->h_dir[i] = SMap{sv->maps[i].table, sv->maps[i].sp, 0};
+  cudaStream_t s = sv->s;
+  HX_CUDA(cudaMemcpyAsync(sv->d_maps, sl->h_dir, sv->maps.size() * sizeof(SMap), cudaMemcpyHostToDevice, s));
+  HX_CUDA(cudaMemcpyAsync(sl->d_reqs, sl->h_reqs, nreq * sizeof(SReq), cudaMemcpyHostToDevice, s));
+  HX_CUDA(cudaMemcpyAsync(sl->d_tiles, sl->h_tiles, ntiles * sizeof(STile), cudaMemcpyHostToDevice, s));
+  HX_CUDA(cudaMemsetAsync(sl->d_cnt, 0, 2 * sizeof(unsigned), s));
+  HX_CUDA(cudaMemcpyAsync(sl->d_cnt + 2, sl->h_rem, nreq * sizeof(unsigned), cudaMemcpyHostToDevice, s));
+  const unsigned tiles_grid = (unsigned)(sm_count() * blocks_per_sm(k_serve<P64>, 256));
+  const unsigned grid = std::min<unsigned>(tiles_grid, ntiles);
+  if (sv->kb == 4) {
+    ServeArgs<P32> a{sv->d_maps, sv->d_info, sl->d_reqs, sl->d_tiles, ntiles, sl->d_cnt, sl->d_cnt + 1, sl->d_cnt + 2};
+    k_serve<P32><<<grid, 256, 0, s>>>(a);
+  } else {
+    ServeArgs<P64> a{sv->d_maps, sv->d_info, sl->d_reqs, sl->d_tiles, ntiles, sl->d_cnt, sl->d_cnt + 1, sl->d_cnt + 2};
+    k_serve<P64><<<grid, 256, 0, s>>>(a);
+  }
+  st = after_launch();
+  if (st != HX_OK) return st;
+  HX_CUDA(cudaMemcpyAsync(sl->h_info, sv->d_info, sv->maps.size() * sizeof(DInfo), cudaMemcpyDeviceToHost, s));
+  HX_CUDA(cudaMemcpyAsync(sl->h_err, sl->d_cnt + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  HX_CUDA(cudaEventRecord(sl->done, s));
+  sl->busy = true;
+  sl->round_no = sv->rounds++;
+  sl->n_maps = sv->maps.size();
+  if (launched) *launched = nreq;
+  return HX_OK;
+}
+
+hx_status hx_server_poll(hx_server* sv, hx_completion* out, uint32_t capacity, uint32_t* n_out) {
+  if (!sv || !n_out || (capacity && !out)) return HX_ERR_INVALID_ARG;
+  hx_status st = reap(sv, false);
+  if (st != HX_OK) return st;
+  const uint32_t n = (uint32_t)std::min<size_t>(capacity, sv->done.size());
+  for (uint32_t i = 0; i < n; ++i) out[i] = sv->done[i];
+  sv->done.erase(sv->done.begin(), sv->done.begin() + n);
+  *n_out = n;
+  return HX_OK;
+}
+
+hx_status hx_server_drain(hx_server* sv) {
+  if (!sv) return HX_ERR_INVALID_ARG;
+  for (;;) {
+    uint32_t launched = 0;
+    hx_status st = hx_server_step(sv, &launched);
+    if (st != HX_OK) return st;
+    bool busy = false;
+    for (auto& sl : sv->slots) busy |= sl.busy;
+    if (sv->queue.empty() && !busy) return HX_OK;
+    if (!launched) {
+      st = reap(sv, true);
+      if (st != HX_OK) return st;
+    }
+  }
+}
+
+hx_status hx_server_map_info(hx_server* sv, uint32_t map, hx_info* out) {
+  if (!sv || !out || map >= sv->maps.size()) return HX_ERR_INVALID_ARG;
+  hx_map v;
+  view_of(sv, map, &v);
+  return hx_get_info(&v, out, sv->s);
+}
+
+hx_status hx_server_bucket_data(hx_server* sv, uint32_t map, void** d_buckets, uint64_t* bucket_count) {
+  if (!sv || map >= sv->maps.size()) return HX_ERR_INVALID_ARG;
+  if (d_buckets) *d_buckets = sv->maps[map].table;
+  if (bucket_count) *bucket_count = 1ull << sv->maps[map].sp;
+  return HX_OK;
+}
+
+hx_status hx_server_memory(hx_server* sv, uint64_t* used, uint64_t* budget) {
+  if (!sv) return HX_ERR_INVALID_ARG;
+  if (used) *used = sv->used;
+  if (budget) *budget = sv->budget;
+  return HX_OK;
+}
+
+hx_status hx_server_run_trace(hx_server* sv, const hx_request* reqs, const uint64_t* arrival_ns, uint32_t count,
+                              uint64_t* complete_ns, int32_t* status, uint64_t* t_start_ns) {
+  if (!sv || (count && (!reqs || !arrival_ns || !complete_ns || !status))) return HX_ERR_INVALID_ARG;
+  for (uint32_t i = 0; i < count; ++i) {
+    complete_ns[i] = 0;
+    status[i] = -1;
+  }
+  // tags are trace indices
+  std::vector<hx_request> rq(reqs, reqs + count);
+  for (uint32_t i = 0; i < count; ++i) rq[i].tag = i;
+  HX_CUDA(cudaStreamSynchronize(sv->s));
+  HX_CUDA(cudaEventRecord(sv->t0, sv->s));
+  sv->t0_ns = now_ns();
+  sv->t0_set = true;
+  const uint64_t start = sv->t0_ns;
+  if (t_start_ns) *t_start_ns = start;
+  uint32_t next = 0, completed = 0;
+  std::vector<hx_completion> buf(4096);
+  while (completed < count) {
+    const uint64_t now = now_ns() - start;
+    uint32_t first = next;
+    while (next < count && arrival_ns[next] <= now) ++next;
+    if (next > first) {
+      hx_status st = hx_server_submit(sv, rq.data() + first, next - first);
+      if (st != HX_OK) return st;
+    }
+    uint32_t launched = 0;
+    hx_status st = hx_server_step(sv, &launched);
+    if (st != HX_OK) return st;
+    uint32_t n = 0;
+    do {
+      st = hx_server_poll(sv, buf.data(), (uint32_t)buf.size(), &n);
+      if (st != HX_OK) return st;
+      for (uint32_t i = 0; i < n; ++i) {
+        const uint64_t tag = buf[i].tag;
+        if (tag < count) {
+          complete_ns[tag] = buf[i].complete_ns - start;
+          status[tag] = buf[i].status;
+          ++completed;
+        }
+      }
+    } while (n == buf.size());
+  }
+  return HX_OK;
+}
+
+}  // extern "C"

@@ -189,3 +189,54 @@ def batched_workload(n_maps: int, seed: int, log_lo: float = 6.0, log_hi: float 
 
     return {"size_powers": sp, "n": n, "keys": keys, "vals": vals, "ins_offsets": offs(n), "queries": queries,
             "query_offsets": offs(nq), "erase": erase, "erase_offsets": offs(n_er)}
+
+
+def serving_trace(n_maps: int, n_requests: int, seed: int, init_log=(8.0, 20.0), size_log=(0.0, 16.0),
+                  mix=(0.2, 0.7, 0.1), present: float = 0.8, rate_req_s: float = 1e6, width: int = 8,
+                  init_lf: float = 0.5):
+    """Serving workload: n_maps maps with initial key counts 2^U, U ~ U[init_log], tables sized for
+    init_lf; then n_requests requests with Poisson arrivals at rate_req_s, each on a uniform random map,
+    2^U keys (U ~ U[size_log], at least 1), op insert/query/erase with probabilities `mix`. Inserts bring
+    fresh keys; queries draw `present` of their keys from keys inserted so far and the rest fresh
+    (absent); erases draw from keys inserted so far. Map i's keys are positions [i*2^40, ...) of one
+    bijective key stream, so maps never share keys. Returns a dict of flat host arrays."""
+    rng = np.random.default_rng(seed)
+    n0 = np.rint(2.0 ** rng.uniform(init_log[0], init_log[1], size=n_maps)).astype(np.int64)
+    sp = np.maximum(np.ceil(np.log2(n0 / init_lf)), 2).astype(np.int32)
+    base = np.arange(n_maps, dtype=np.uint64) << np.uint64(40)
+    fresh = n0.copy()  # next unused stream position per map
+    req_map = rng.integers(0, n_maps, size=n_requests)
+    req_op = rng.choice(3, size=n_requests, p=list(mix))
+    req_n = np.maximum(np.rint(2.0 ** rng.uniform(size_log[0], size_log[1], size=n_requests)), 1).astype(np.int64)
+    pos_parts = []
+    for i in range(n_requests):
+        m, op, k = int(req_map[i]), int(req_op[i]), int(req_n[i])
+        if op == 0:
+            pos = np.arange(fresh[m], fresh[m] + k, dtype=np.int64)
+            fresh[m] += k
+        elif op == 1:
+            n_p = int(rng.binomial(k, present))
+            pos = np.concatenate([rng.integers(0, fresh[m], size=n_p),
+                                  np.arange(fresh[m] + (1 << 30), fresh[m] + (1 << 30) + (k - n_p), dtype=np.int64)])
+            rng.shuffle(pos)
+        else:
+            pos = rng.integers(0, fresh[m], size=k)
+        pos_parts.append(pos.astype(np.uint64) + base[m])
+    init_pos = np.concatenate([np.arange(n, dtype=np.uint64) + base[m] for m, n in enumerate(n0)])
+    init_off = np.zeros(n_maps + 1, np.int64)
+    init_off[1:] = np.cumsum(n0)
+    req_off = np.zeros(n_requests + 1, np.int64)
+    req_off[1:] = np.cumsum(req_n)
+    req_pos = np.concatenate(pos_parts) if pos_parts else np.zeros(0, np.uint64)
+    gaps = rng.exponential(1e9 / rate_req_s, size=n_requests)
+    arrival = np.cumsum(gaps).astype(np.uint64)
+    dt = np.uint32 if width == 4 else np.uint64
+
+    def keys_of(pos):
+        return keys_at(pos, width, seed).astype(dt) if len(pos) else np.zeros(0, dt)
+
+    return {"size_powers": sp, "n0": n0, "init_keys": keys_of(init_pos),
+            "init_vals": values(len(init_pos), width, seed + 11), "init_offsets": init_off,
+            "req_map": req_map.astype(np.uint32), "req_op": req_op.astype(np.uint32), "req_n": req_n,
+            "req_offsets": req_off, "req_keys": keys_of(req_pos), "req_vals": values(len(req_pos), width, seed + 12),
+            "arrival_ns": arrival}

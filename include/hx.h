@@ -283,6 +283,58 @@ hx_status hx_batch_check(hx_batch_plan* plan, int32_t* error, hx_stream stream);
  * Phases: 0 insert, 1 query, 2 erase, 3..5 clean_tombstones. Synchronises. */
 hx_status hx_batch_inject_stall(hx_batch_plan* plan, uint32_t map, int phase, int enable, hx_stream stream);
 
+/* ---- serving loop ------------------------------------------------------- */
+/* No reference counterpart (the reference has no request loop). A server
+ * keeps many maps resident and runs queued requests in rounds: one fused
+ * launch per round, requests on different maps concurrently, requests on the
+ * same map in admission order, several rounds in flight (the host forms the
+ * next round while the GPU runs the current one). Before a round, a map
+ * whose load factor would pass max_load_factor is grown by an on-device
+ * rehash; tables are admitted against memory_budget_bytes, and an insert
+ * that cannot grow its table within the budget completes with HX_ERR_OOM.
+ * One host thread drives a server. */
+typedef struct hx_server hx_server;
+enum { HX_OP_INSERT = 0, HX_OP_QUERY = 1, HX_OP_ERASE = 2 };
+typedef struct hx_request {
+  uint32_t map;
+  uint32_t op;       /* HX_OP_*: insert keys+vals, query keys -> out (misses untouched), erase keys */
+  const void* keys;  /* device arrays, alive until the request completes */
+  const void* vals;
+  void* out;
+  uint64_t n;
+  uint64_t tag;      /* returned in the completion */
+} hx_request;
+typedef struct hx_completion {
+  uint64_t tag;
+  uint64_t complete_ns; /* host steady-clock ns of the end of the request's round */
+  int32_t status;       /* HX_OK, HX_ERR_OOM (insert not admitted), HX_ERR_TIMEOUT */
+  int32_t reserved;
+} hx_completion;
+
+hx_status hx_server_create(hx_server** out, int key_bytes, uint64_t memory_budget_bytes, float max_load_factor,
+                           uint32_t max_maps, uint32_t max_round_requests, uint64_t max_round_keys,
+                           uint32_t rounds_in_flight);
+hx_status hx_server_destroy(hx_server* server);
+/* A new empty map of 2^size_power buckets, if it fits the budget (else HX_ERR_OOM). */
+hx_status hx_server_add_map(hx_server* server, int size_power, uint32_t* map_id);
+hx_status hx_server_submit(hx_server* server, const hx_request* requests, uint32_t count);
+/* Forms and launches one round from the queue if a round slot is free;
+ * *launched = requests in it (0 if none). Never blocks on the GPU. */
+hx_status hx_server_step(hx_server* server, uint32_t* launched);
+/* Completions since the last poll (at most capacity). */
+hx_status hx_server_poll(hx_server* server, hx_completion* out, uint32_t capacity, uint32_t* n_out);
+/* Runs until the queue is empty and every round has completed. */
+hx_status hx_server_drain(hx_server* server);
+hx_status hx_server_map_info(hx_server* server, uint32_t map, hx_info* out);
+hx_status hx_server_bucket_data(hx_server* server, uint32_t map, void** d_buckets, uint64_t* bucket_count);
+hx_status hx_server_memory(hx_server* server, uint64_t* used, uint64_t* budget);
+/* Replays a request trace in real time: request i is submitted once
+ * arrival_ns[i] (ns after the start, non-decreasing) has passed; returns
+ * when all requests completed, with complete_ns[i] (ns after the start) and
+ * status[i]. The loop is native so arrivals are not limited by a caller. */
+hx_status hx_server_run_trace(hx_server* server, const hx_request* requests, const uint64_t* arrival_ns,
+                              uint32_t count, uint64_t* complete_ns, int32_t* status, uint64_t* t_start_ns);
+
 /* Exclusive u32 scan that allocates nothing. No counterpart in the
  * reference: it is hx_exclusive_scan_u32 for callers that may not allocate
  * device memory when they scan (a host framework that owns all device memory,
