@@ -212,6 +212,60 @@ def run_batched(args, stream, dev):
             "timing": "CUDA events around clear + run, median; fused replays a captured CUDA graph"}
 
 
+def run_serving(args, dev):
+    """1024 resident u64 maps (initial key counts log-uniform in [2^8, 2^20], tables at LF <= 0.5), a 40 GB
+    device-memory budget, on-device growth past LF 0.8; Poisson arrivals at swept rates, requests of
+    log-uniform 1..2^16 keys, insert/query/erase 20/70/10, queries 80% present. Each rate starts from the
+    same initial maps; the native loop submits each request at its arrival time."""
+    import torch
+    import hashinator_gb300 as hx
+    from hashinator_gb300 import workloads
+    t0 = time.perf_counter()
+    base_rate = 1e6
+    tr = workloads.serving_trace(args.serving_maps, args.serving_requests, 5, init_log=(8.0, 20.0),
+                                 size_log=(0.0, 16.0), rate_req_s=base_rate, width=8)
+    gen_s = time.perf_counter() - t0
+
+    def dev64(a):
+        return torch.from_numpy(a.view(np.int64)).to(dev)
+
+    ik, iv, rk, rv = dev64(tr["init_keys"]), dev64(tr["init_vals"]), dev64(tr["req_keys"]), dev64(tr["req_vals"])
+    out = torch.empty(len(tr["req_keys"]), dtype=torch.int64, device=dev)
+    io, ro = tr["init_offsets"], tr["req_offsets"]
+    n_req = len(tr["req_map"])
+    total_keys = int(ro[-1])
+    results = []
+    for rate in args.serving_rates:
+        srv = hx.Server(key_bytes=8, memory_budget=40 << 30, max_load_factor=0.8, max_maps=args.serving_maps,
+                        max_round_requests=4096, max_round_keys=1 << 23, rounds_in_flight=3)
+        ids = [srv.add_map(int(sp)) for sp in tr["size_powers"]]
+        srv.submit([(ids[m], hx.OP_INSERT, ik.data_ptr() + int(io[m]) * 8, iv.data_ptr() + int(io[m]) * 8, 0,
+                     int(io[m + 1] - io[m]), m) for m in range(len(ids))])
+        srv.drain()
+        srv.poll()
+        torch.cuda.synchronize()
+        reqs = srv.requests([(ids[int(tr["req_map"][i])], int(tr["req_op"][i]), rk.data_ptr() + int(ro[i]) * 8,
+                              rv.data_ptr() + int(ro[i]) * 8, out.data_ptr() + int(ro[i]) * 8, int(tr["req_n"][i]), i)
+                             for i in range(n_req)])
+        arrival = (tr["arrival_ns"].astype(np.float64) * (base_rate / rate)).astype(np.uint64)
+        comp, st = srv.run_trace(reqs, arrival)
+        lat = (comp.astype(np.float64) - arrival.astype(np.float64)) / 1e3
+        span = (comp.max() - arrival.min()) / 1e9
+        used, _ = srv.memory()
+        results.append({"offered_req_s": rate, "offered_Mkeys_s": round(total_keys / (arrival.max() / 1e9) / 1e6, 1),
+                        "p50_us": round(float(np.percentile(lat, 50)), 1),
+                        "p99_us": round(float(np.percentile(lat, 99)), 1),
+                        "sustained_Mkeys_s": round(total_keys / span / 1e6, 1),
+                        "ok": int((st == 0).sum()), "rejected": int((st != 0).sum()),
+                        "device_GB": round(used / 1e9, 2)})
+        srv.close()
+    return {"workload": f"{args.serving_maps} u64 maps, initial keys log-uniform [2^8, 2^20], 40 GB budget, grow "
+                        f"past LF 0.8; {n_req} Poisson requests of log-uniform 1..2^16 keys, insert/query/erase "
+                        f"20/70/10, queries 80% present",
+            "keys_per_run": total_keys, "initial_keys": int(io[-1]), "rates": results, "generate_s": round(gen_s, 1),
+            "latency": "arrival (host clock) to the end of the request's round (CUDA event on the serving stream)"}
+
+
 def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -439,6 +493,9 @@ def run_ours(args):
     batched = None
     if not args.no_batched:
         batched = run_batched(args, stream, dev)
+    serving = None
+    if not args.no_serving:
+        serving = run_serving(args, dev)
 
     if rank == 0:
         metric = METRIC if args.log_keys == 26 else METRIC.replace("2^26 keys, 2^27", f"2^{args.log_keys} keys, 2^{sp}")
@@ -452,7 +509,7 @@ def run_ours(args):
                            "l2": "inputs larger than L2 (1 GiB table, 256 MiB arrays); no flush",
                            "group_width": args.group or "default"},
                 "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
-                "batched": batched,
+                "batched": batched, "serving": serving,
                 "clocks": clocks}
         print(json.dumps(line), flush=True)
     m.close()
@@ -473,6 +530,10 @@ def main():
     ap.add_argument("--e2e-chunks", type=int, default=8)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-maps", type=int, default=4096)
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serving-maps", type=int, default=1024)
+    ap.add_argument("--serving-requests", type=int, default=20000)
+    ap.add_argument("--serving-rates", type=float, nargs="+", default=[2.5e5, 5e5, 1e6, 2e6, 4e6])
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
