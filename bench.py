@@ -252,7 +252,9 @@ def run_serving(args, dev):
         lat = (comp.astype(np.float64) - arrival.astype(np.float64)) / 1e3
         span = (comp.max() - arrival.min()) / 1e9
         used, _ = srv.memory()
-        results.append({"offered_req_s": rate, "offered_Mkeys_s": round(total_keys / (arrival.max() / 1e9) / 1e6, 1),
+        sst = srv.stats()
+        results.append({"rounds": sst["rounds"], "growths": sst["growths"], "max_stage_depth": sst["max_stage_depth"],
+                        "host_ms_forming_rounds": round(sst["host_ns_step"] / 1e6, 1),"offered_req_s": rate, "offered_Mkeys_s": round(total_keys / (arrival.max() / 1e9) / 1e6, 1),
                         "p50_us": round(float(np.percentile(lat, 50)), 1),
                         "p99_us": round(float(np.percentile(lat, 99)), 1),
                         "sustained_Mkeys_s": round(total_keys / span / 1e6, 1),

@@ -91,6 +91,14 @@ class Completion(ctypes.Structure):
 
 OP_INSERT, OP_QUERY, OP_ERASE = 0, 1, 2
 
+
+class ServerStats(ctypes.Structure):
+    """hx_server_stats."""
+    _fields_ = [("rounds", ctypes.c_uint64), ("requests", ctypes.c_uint64), ("keys", ctypes.c_uint64),
+                ("growths", ctypes.c_uint64), ("growth_bytes", ctypes.c_uint64), ("rejected", ctypes.c_uint64),
+                ("timeouts", ctypes.c_uint64), ("host_ns_step", ctypes.c_uint64), ("max_stage_depth", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
 _lib_handle = None
 
 _SIGS = {
@@ -152,6 +160,7 @@ _SIGS.update({
     "hx_server_bucket_data": [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p),
                               ctypes.POINTER(ctypes.c_uint64)],
     "hx_server_memory": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)],
+    "hx_server_get_stats": [ctypes.c_void_p, ctypes.POINTER(ServerStats)],
     "hx_server_run_trace": [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_void_p, ctypes.c_uint32,
                             ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)],
 })
@@ -608,6 +617,11 @@ class Server:
         u, b = ctypes.c_uint64(), ctypes.c_uint64()
         _check(self._h.hx_server_memory(self._s, ctypes.byref(u), ctypes.byref(b)), "hx_server_memory")
         return u.value, b.value
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(self._h.hx_server_get_stats(self._s, ctypes.byref(st)), "hx_server_get_stats")
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_ if k != "reserved"}
 
     def run_trace(self, reqs, arrival_ns):
         """Real-time replay; returns (complete_ns, status) numpy arrays."""

@@ -38,8 +38,8 @@ struct SReq {
   unsigned long long n;
   unsigned map;
   unsigned op;
-  int prev;  // previous request on the same map in this round, or -1
-  unsigned pad;
+  int wait;        // stage this request waits for (the map's previous stage), or -1
+  unsigned stage;  // stage whose counter this request's tiles count off
 };
 struct STile {
   unsigned req;
@@ -61,7 +61,7 @@ struct ServeArgs {
   unsigned n_tiles;
   unsigned* work;
   unsigned* error;
-  unsigned* remaining;  // tiles left per request
+  unsigned* remaining;  // tiles left per stage
 };
 
 constexpr unsigned long long kServeWaitNs = 1000000000ull;
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(256) k_serve(ServeArgs<P> a) {
       if (!s_end) {
         s_t = a.tiles[idx];
         s_r = a.reqs[s_t.req];
-        if (s_r.prev >= 0 && !serve_wait_zero(a.remaining + s_r.prev)) {
+        if (s_r.wait >= 0 && !serve_wait_zero(a.remaining + s_r.wait)) {
           s_ok = 0;
           atomicExch(a.error, 1u);
         }
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(256) k_serve(ServeArgs<P> a) {
         atomicAdd(&inf->fill, 0ull - (unsigned long long)s_erased);
       }
       __threadfence();
-      atomicSub(a.remaining + t.req, 1u);
+      atomicSub(a.remaining + r.stage, 1u);
     }
   }
 }
@@ -254,6 +254,7 @@ struct hx_server {
   bool t0_set = false;
   std::vector<hx_completion> done;  // completed since the last poll
   uint64_t timeouts = 0;
+  hx_server_stats st{};
 };
 
 namespace hx {
@@ -287,7 +288,10 @@ static hx_status reap(hx_server* sv, bool wait_oldest) {
     if (sv->t0_set) cudaEventElapsedTime(&ms, sv->t0, sl.done);
     const uint64_t t_ns = sv->t0_ns + (uint64_t)((double)ms * 1e6);
     const int32_t st = *sl.h_err ? HX_ERR_TIMEOUT : HX_OK;
-    if (*sl.h_err) sv->timeouts++;
+    if (*sl.h_err) {
+      sv->timeouts++;
+      sv->st.timeouts++;
+    }
     for (uint64_t tag : sl.tags) sv->done.push_back(hx_completion{tag, t_ns, st, 0});
     for (auto& ins : sl.inserts) sv->maps[ins.first].in_flight -= ins.second;
     for (size_t i = 0; i < sl.n_maps && i < sv->maps.size(); ++i)
@@ -320,8 +324,19 @@ hx_status hx_server_create(hx_server** out, int key_bytes, uint64_t memory_budge
   sv->max_maps = max_maps;
   sv->max_round_requests = max_round_requests;
   sv->max_round_keys = max_round_keys;
-  const uint64_t max_tiles = max_round_requests + max_round_keys / sv->tile_keys + 1;
+  const uint64_t max_tiles = max_round_requests + max_round_keys / 256 + 1;
   cudaError_t e = cudaStreamCreateWithFlags(&sv->s, cudaStreamNonBlocking);
+  // Tables grow and shrink through the stream-ordered allocator: keep freed
+  // memory in the device's default pool instead of returning it to the
+  // driver at every synchronisation (a process-local pool attribute).
+  {
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetDefaultMemPool(&pool, dev);
+    uint64_t keep = ~0ull;
+    if (e == cudaSuccess) e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&sv->d_maps), max_maps * sizeof(SMap));
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&sv->d_info), max_maps * sizeof(DInfo));
   if (e == cudaSuccess) e = cudaEventCreate(&sv->t0);
@@ -412,8 +427,17 @@ hx_status hx_server_submit(hx_server* sv, const hx_request* reqs, uint32_t count
   return HX_OK;
 }
 
+static hx_status server_step(hx_server* sv, uint32_t* launched);
+
 hx_status hx_server_step(hx_server* sv, uint32_t* launched) {
   if (!sv) return HX_ERR_INVALID_ARG;
+  const uint64_t t0 = now_ns();
+  hx_status st = server_step(sv, launched);
+  sv->st.host_ns_step += now_ns() - t0;
+  return st;
+}
+
+static hx_status server_step(hx_server* sv, uint32_t* launched) {
   if (launched) *launched = 0;
   hx_status st = reap(sv, false);
   if (st != HX_OK) return st;
@@ -461,23 +485,45 @@ hx_status hx_server_step(hx_server* sv, uint32_t* launched) {
       st = map_rehash_view(&v, nsp, sv->s);  // on-device rehash, stream-ordered after earlier rounds
       if (st != HX_OK) return st;
       sv->used = sv->used - m.bytes + nbytes;
+      sv->st.growths++;
+      sv->st.growth_bytes += nbytes;
       m.table = v.buckets;
       m.sp = nsp;
       m.bytes = nbytes;
     }
     add[r.map] += r.n;
   }
-  // Chain requests per map, order tiles by rank within the map.
-  std::vector<int> last(sv->maps.size(), -1), rank_of(sv->maps.size(), 0);
-  std::vector<std::pair<int, unsigned>> order;  // (rank, request index in round)
+  // Stages per map, in admission order: a write (insert, erase) is a stage of
+  // its own; consecutive queries share one stage. Every stage waits for the
+  // map's previous stage, so reads never see later writes and writes never
+  // overtake earlier reads, while queries between two writes run together.
+  std::vector<int> cur_stage(sv->maps.size(), -1), cur_depth(sv->maps.size(), -1);
+  std::vector<char> cur_is_query(sv->maps.size(), 0);
+  std::vector<int> stage_depth;
+  std::vector<std::pair<int, unsigned>> order;  // (stage depth, request index in round)
   unsigned nreq = 0;
+  uint64_t round_keys = 0;
   sl->tags.clear();
   sl->inserts.clear();
   for (size_t i = 0; i < round.size(); ++i) {
     const hx_request& r = round[i].r;
     if (!admitted[i]) {
       sv->done.push_back(hx_completion{r.tag, now_ns(), HX_ERR_OOM, 0});
+      sv->st.rejected++;
       continue;
+    }
+    const bool query = r.op == SOP_QUERY;
+    int wait, stage;
+    if (query && cur_stage[r.map] >= 0 && cur_is_query[r.map]) {
+      stage = cur_stage[r.map];  // join the running group of queries
+      wait = -2;                 // filled below from the stage's own wait
+    } else {
+      wait = cur_stage[r.map];
+      stage = (int)stage_depth.size();
+      stage_depth.push_back(cur_depth[r.map] + 1);
+      cur_stage[r.map] = stage;
+      cur_depth[r.map] += 1;
+      cur_is_query[r.map] = query ? 1 : 0;
     }
     SReq q;
     q.keys = r.keys;
@@ -486,30 +532,50 @@ hx_status hx_server_step(hx_server* sv, uint32_t* launched) {
     q.n = r.n;
     q.map = r.map;
     q.op = r.op;
-    q.prev = last[r.map];
-    q.pad = 0;
-    last[r.map] = (int)nreq;
+    q.wait = wait;
+    q.stage = (unsigned)stage;
+    if (wait == -2) {
+      // same wait as the first request of this stage
+      for (int j = (int)nreq - 1; j >= 0; --j)
+        if (sl->h_reqs[j].stage == (unsigned)stage && sl->h_reqs[j].wait != -2) {
+          q.wait = sl->h_reqs[j].wait;
+          break;
+        }
+    }
     sl->h_reqs[nreq] = q;
-    order.push_back({rank_of[r.map]++, nreq});
+    order.push_back({stage_depth[stage], nreq});
     sl->tags.push_back(r.tag);
     if (r.op == SOP_INSERT && r.n) sl->inserts.push_back({r.map, r.n});
+    round_keys += r.n;
     ++nreq;
   }
   if (nreq == 0) return HX_OK;
   std::stable_sort(order.begin(), order.end(),
                    [](const std::pair<int, unsigned>& a, const std::pair<int, unsigned>& b) { return a.first < b.first; });
+  // Tile size: enough tiles to spread one round over every SM, 256..4096 keys.
+  const uint64_t spread = (uint64_t)sm_count() * 8;
+  uint64_t tile = 256;
+  while (tile < 4096 && tile * spread < round_keys) tile *= 2;
+  const unsigned nstages = (unsigned)stage_depth.size();
+  for (unsigned j = 0; j < nstages; ++j) sl->h_rem[j] = 0;
   unsigned ntiles = 0;
+  int max_depth = 0;
   for (auto& o : order) {
     const SReq& q = sl->h_reqs[o.second];
+    max_depth = std::max(max_depth, o.first);
     unsigned nt = 0;
-    for (uint64_t a0 = 0; a0 < q.n || nt == 0; a0 += sv->tile_keys) {
-      const uint64_t c = q.n > a0 ? std::min<uint64_t>(sv->tile_keys, q.n - a0) : 0;
+    for (uint64_t a0 = 0; a0 < q.n || nt == 0; a0 += tile) {
+      const uint64_t c = q.n > a0 ? std::min<uint64_t>(tile, q.n - a0) : 0;
       sl->h_tiles[ntiles++] = STile{o.second, (unsigned)c, a0};
       ++nt;
       if (q.n == 0) break;
     }
-    sl->h_rem[o.second] = nt;
+    sl->h_rem[q.stage] += nt;
   }
+  sv->st.rounds++;
+  sv->st.requests += nreq;
+  sv->st.keys += round_keys;
+  sv->st.max_stage_depth = std::max<uint32_t>(sv->st.max_stage_depth, (uint32_t)max_depth);
   for (auto& x : sl->inserts) sv->maps[x.first].in_flight += x.second;
   for (size_t i = 0; i < sv->maps.size(); ++i) sl->h_dir[i] = SMap{sv->maps[i].table, sv->maps[i].sp, 0};
   cudaStream_t s = sv->s;
@@ -517,7 +583,7 @@ hx_status hx_server_step(hx_server* sv, uint32_t* launched) {
   HX_CUDA(cudaMemcpyAsync(sl->d_reqs, sl->h_reqs, nreq * sizeof(SReq), cudaMemcpyHostToDevice, s));
   HX_CUDA(cudaMemcpyAsync(sl->d_tiles, sl->h_tiles, ntiles * sizeof(STile), cudaMemcpyHostToDevice, s));
   HX_CUDA(cudaMemsetAsync(sl->d_cnt, 0, 2 * sizeof(unsigned), s));
-  HX_CUDA(cudaMemcpyAsync(sl->d_cnt + 2, sl->h_rem, nreq * sizeof(unsigned), cudaMemcpyHostToDevice, s));
+  HX_CUDA(cudaMemcpyAsync(sl->d_cnt + 2, sl->h_rem, nstages * sizeof(unsigned), cudaMemcpyHostToDevice, s));
   const unsigned tiles_grid = (unsigned)(sm_count() * blocks_per_sm(k_serve<P64>, 256));
   const unsigned grid = std::min<unsigned>(tiles_grid, ntiles);
   if (sv->kb == 4) {
@@ -577,6 +643,12 @@ hx_status hx_server_bucket_data(hx_server* sv, uint32_t map, void** d_buckets, u
   if (!sv || map >= sv->maps.size()) return HX_ERR_INVALID_ARG;
   if (d_buckets) *d_buckets = sv->maps[map].table;
   if (bucket_count) *bucket_count = 1ull << sv->maps[map].sp;
+  return HX_OK;
+}
+
+hx_status hx_server_get_stats(hx_server* sv, hx_server_stats* out) {
+  if (!sv || !out) return HX_ERR_INVALID_ARG;
+  *out = sv->st;
   return HX_OK;
 }
 

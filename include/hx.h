@@ -328,6 +328,15 @@ hx_status hx_server_drain(hx_server* server);
 hx_status hx_server_map_info(hx_server* server, uint32_t map, hx_info* out);
 hx_status hx_server_bucket_data(hx_server* server, uint32_t map, void** d_buckets, uint64_t* bucket_count);
 hx_status hx_server_memory(hx_server* server, uint64_t* used, uint64_t* budget);
+typedef struct hx_server_stats {
+  uint64_t rounds, requests, keys;  /* launched */
+  uint64_t growths, growth_bytes;   /* on-device rehashes and the bytes of their new tables */
+  uint64_t rejected, timeouts;
+  uint64_t host_ns_step;            /* host time spent forming and launching rounds */
+  uint32_t max_stage_depth;         /* longest per-map dependency chain in a round */
+  uint32_t reserved;
+} hx_server_stats;
+hx_status hx_server_get_stats(hx_server* server, hx_server_stats* out);
 /* Replays a request trace in real time: request i is submitted once
  * arrival_ns[i] (ns after the start, non-decreasing) has passed; returns
  * when all requests completed, with complete_ns[i] (ns after the start) and
