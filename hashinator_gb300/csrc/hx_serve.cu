@@ -11,11 +11,13 @@
 // Several rounds are in flight at once: the host forms round k+1 while the
 // GPU runs round k, and requests that arrive meanwhile join the next round.
 //
-// Every table stays resident. Before a round, a map whose load factor would
-// pass the limit after the round's inserts is grown by an on-device rehash
-// (device_rehash, hashinator.h:285-336) into a table allocated against the
-// server's device-memory budget; an insert that cannot be admitted within the
-// budget is rejected and reported, the map's other requests proceed.
+// Every table stays resident. Before a round, a map whose occupancy (keys plus
+// tombstones, which insert never reuses) would pass the load-factor limit is
+// rehashed on the device (device_rehash, hashinator.h:285-336): tombstones
+// are dropped and the table grows only if its live keys need it, allocated
+// against the server's device-memory budget. An insert that cannot be given
+// room within the budget is rejected and reported; the map's other requests
+// proceed.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -204,8 +206,11 @@ struct ServeMap {
   int sp = 0;
   void* table = nullptr;
   uint64_t bytes = 0;
-  uint64_t fill_ub = 0;    // upper bound of fill once every launched round is done
-  uint64_t in_flight = 0;  // inserts launched in rounds not yet completed
+  uint64_t fill_ub = 0;          // upper bound of fill once every launched round is done
+  uint64_t tomb_ub = 0;          // upper bound of tombstones once every launched round is done
+  uint64_t in_flight = 0;        // inserts launched in rounds not yet completed
+  uint64_t in_flight_erase = 0;  // erase keys launched in rounds not yet completed
+  uint64_t rehash_round = 0;     // first round that runs on the current table
 };
 
 struct Pending {
@@ -229,6 +234,7 @@ struct Slot {
   cudaEvent_t done = nullptr;
   std::vector<uint64_t> tags;
   std::vector<std::pair<unsigned, uint64_t>> inserts;  // (map, keys) launched in this round
+  std::vector<std::pair<unsigned, uint64_t>> erases;   // (map, keys) launched in this round
 };
 
 }  // namespace hx
@@ -294,11 +300,17 @@ static hx_status reap(hx_server* sv, bool wait_oldest) {
     }
     for (uint64_t tag : sl.tags) sv->done.push_back(hx_completion{tag, t_ns, st, 0});
     for (auto& ins : sl.inserts) sv->maps[ins.first].in_flight -= ins.second;
-    for (size_t i = 0; i < sl.n_maps && i < sv->maps.size(); ++i)
-      sv->maps[i].fill_ub = sl.h_info[i].fill + sv->maps[i].in_flight;
+    for (auto& er : sl.erases) sv->maps[er.first].in_flight_erase -= er.second;
+    for (size_t i = 0; i < sl.n_maps && i < sv->maps.size(); ++i) {
+      ServeMap& m = sv->maps[i];
+      m.fill_ub = sl.h_info[i].fill + m.in_flight;  // a rehash keeps fill
+      // tombstones of a snapshot taken before the map's last rehash are gone
+      if (sl.round_no >= m.rehash_round) m.tomb_ub = sl.h_info[i].tombstones + m.in_flight_erase;
+    }
     sl.busy = false;
     sl.tags.clear();
     sl.inserts.clear();
+    sl.erases.clear();
   }
   return HX_OK;
 }
@@ -464,20 +476,32 @@ static hx_status server_step(hx_server* sv, uint32_t* launched) {
     round.push_back(p);
     sv->queue.pop_front();
   }
-  // Growth and admission of inserts, in admission order.
-  std::vector<uint64_t> add(sv->maps.size(), 0);
+  // Table maintenance and admission of inserts, in admission order. Insert
+  // never reuses TOMBSTONE buckets (kernels_NVIDIA.h:383-407), so a map whose
+  // fill + tombstones + incoming keys would pass the load-factor limit is
+  // rehashed first: the rehash drops its tombstones and grows the table only
+  // if the live keys need it. Bounds are upper bounds, so a map never fills.
+  std::vector<uint64_t> add(sv->maps.size(), 0), era(sv->maps.size(), 0);
   std::vector<char> admitted(round.size(), 1);
+  const uint64_t this_round = sv->rounds;
   for (size_t i = 0; i < round.size(); ++i) {
     const hx_request& r = round[i].r;
+    if (r.op == SOP_ERASE) {
+      era[r.map] += r.n;
+      continue;
+    }
     if (r.op != SOP_INSERT || r.n == 0) continue;
     ServeMap& m = sv->maps[r.map];
-    const uint64_t proj = m.fill_ub + add[r.map] + r.n;
-    if ((double)proj > (double)sv->max_lf * (double)(1ull << m.sp)) {
+    const double lim = (double)sv->max_lf;
+    const uint64_t occ = m.fill_ub + m.tomb_ub + add[r.map] + era[r.map] + r.n;
+    if ((double)occ > lim * (double)(1ull << m.sp)) {
+      // after a rehash: live keys (bound) + this round's erases and inserts so far + this insert
+      const uint64_t after = m.fill_ub + add[r.map] + era[r.map] + r.n;
       int nsp = m.sp;
-      while ((double)proj > (double)sv->max_lf * (double)(1ull << nsp) && nsp < 31) ++nsp;
+      while ((double)after > lim * (double)(1ull << nsp) && nsp < 31) ++nsp;
       const uint64_t nbytes = (1ull << nsp) * pb(sv);
-      if (sv->used - m.bytes + nbytes > sv->budget || (double)proj > (double)sv->max_lf * (double)(1ull << nsp)) {
-        admitted[i] = 0;  // cannot grow within the budget: reject this insert
+      if ((double)after > lim * (double)(1ull << nsp) || sv->used - m.bytes + nbytes > sv->budget) {
+        admitted[i] = 0;  // cannot make room within the budget: reject this insert
         continue;
       }
       hx_map v;
@@ -490,6 +514,8 @@ static hx_status server_step(hx_server* sv, uint32_t* launched) {
       m.table = v.buckets;
       m.sp = nsp;
       m.bytes = nbytes;
+      m.tomb_ub = 0;
+      m.rehash_round = this_round;
     }
     add[r.map] += r.n;
   }
@@ -546,6 +572,7 @@ static hx_status server_step(hx_server* sv, uint32_t* launched) {
     order.push_back({stage_depth[stage], nreq});
     sl->tags.push_back(r.tag);
     if (r.op == SOP_INSERT && r.n) sl->inserts.push_back({r.map, r.n});
+    if (r.op == SOP_ERASE && r.n) sl->erases.push_back({r.map, r.n});
     round_keys += r.n;
     ++nreq;
   }
@@ -577,6 +604,10 @@ static hx_status server_step(hx_server* sv, uint32_t* launched) {
   sv->st.keys += round_keys;
   sv->st.max_stage_depth = std::max<uint32_t>(sv->st.max_stage_depth, (uint32_t)max_depth);
   for (auto& x : sl->inserts) sv->maps[x.first].in_flight += x.second;
+  for (auto& x : sl->erases) {
+    sv->maps[x.first].in_flight_erase += x.second;
+    sv->maps[x.first].tomb_ub += x.second;
+  }
   for (size_t i = 0; i < sv->maps.size(); ++i) sl->h_dir[i] = SMap{sv->maps[i].table, sv->maps[i].sp, 0};
   cudaStream_t s = sv->s;
   HX_CUDA(cudaMemcpyAsync(sv->d_maps, sl->h_dir, sv->maps.size() * sizeof(SMap), cudaMemcpyHostToDevice, s));

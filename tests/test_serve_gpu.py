@@ -45,6 +45,18 @@ def _setup(hx, t, width=8, **kw):
     return srv, ids, d, init, reqs
 
 
+def _make_room(hm, n, lim=0.8):
+    """The serving maintenance rule with exact counts: rehash (dropping
+    tombstones, growing only if the live keys need it) when fill + tombstones
+    + n would pass the load-factor limit."""
+    inf = hm.info()
+    if inf.fill + inf.tombstone_counter + n > lim * inf.bucket_count:
+        sp = inf.size_power
+        while inf.fill + n > lim * (1 << sp):
+            sp += 1
+        hm.resize(sp)
+
+
 def _replay(hx, t, width, statuses):
     """The requests of each map, one by one in admission order, through hx.Hashmap."""
     dt = np.uint32 if width == 4 else np.uint64
@@ -54,7 +66,8 @@ def _replay(hx, t, width, statuses):
     maps = []
     for m, sp in enumerate(t["size_powers"]):
         hm = hx.Hashmap(int(sp), width)
-        hm.insert(to_dev(t["init_keys"][io[m]:io[m + 1]]), to_dev(t["init_vals"][io[m]:io[m + 1]]), target_lf=0.8)
+        _make_room(hm, int(io[m + 1] - io[m]))
+        hm.insert(to_dev(t["init_keys"][io[m]:io[m + 1]]), to_dev(t["init_vals"][io[m]:io[m + 1]]), target_lf=0.0)
         maps.append(hm)
     for i in range(len(t["req_map"])):
         if statuses is not None and statuses[i] != 0:
@@ -62,7 +75,9 @@ def _replay(hx, t, width, statuses):
         m, op = int(t["req_map"][i]), int(t["req_op"][i])
         k = to_dev(t["req_keys"][ro[i]:ro[i + 1]])
         if op == 0:
-            maps[m].insert(k, to_dev(t["req_vals"][ro[i]:ro[i + 1]]), target_lf=0.8)
+            _make_room(maps[m], int(ro[i + 1] - ro[i]))
+            maps[m].insert(k, to_dev(t["req_vals"][ro[i]:ro[i + 1]]), target_lf=0.0)
+            assert maps[m].peek_status() == hx.STATUS_SUCCESS
         elif op == 1:
             o = to_dev(out[ro[i]:ro[i + 1]])
             maps[m].retrieve(k, o)
@@ -100,7 +115,8 @@ def test_each_result_same_alone_and_in_the_mix(hx, width):
         np.testing.assert_array_equal(k, k2)
         np.testing.assert_array_equal(v, v2)
         inf, inf2 = srv.map_info(ids[m]), maps[m].info()
-        assert inf.fill == inf2.fill and inf.fill / n <= 0.8 + 1e-9
+        assert inf.fill == inf2.fill and (inf.fill + inf.tombstone_counter) / n <= 0.8 + 1e-9
+        assert inf.err != hx.STATUS_FAIL  # no insert ever ran out of buckets
     assert grew > 0  # the trace grew some tables on the device
 
 
