@@ -525,7 +525,7 @@ static hx_status server_step(hx_server* sv, uint32_t* launched) {
   // overtake earlier reads, while queries between two writes run together.
   std::vector<int> cur_stage(sv->maps.size(), -1), cur_depth(sv->maps.size(), -1);
   std::vector<char> cur_is_query(sv->maps.size(), 0);
-  std::vector<int> stage_depth;
+  std::vector<int> stage_depth, stage_wait;
   std::vector<std::pair<int, unsigned>> order;  // (stage depth, request index in round)
   unsigned nreq = 0;
   uint64_t round_keys = 0;
@@ -542,11 +542,12 @@ static hx_status server_step(hx_server* sv, uint32_t* launched) {
     int wait, stage;
     if (query && cur_stage[r.map] >= 0 && cur_is_query[r.map]) {
       stage = cur_stage[r.map];  // join the running group of queries
-      wait = -2;                 // filled below from the stage's own wait
+      wait = stage_wait[stage];
     } else {
       wait = cur_stage[r.map];
       stage = (int)stage_depth.size();
       stage_depth.push_back(cur_depth[r.map] + 1);
+      stage_wait.push_back(wait);
       cur_stage[r.map] = stage;
       cur_depth[r.map] += 1;
       cur_is_query[r.map] = query ? 1 : 0;
@@ -560,14 +561,6 @@ static hx_status server_step(hx_server* sv, uint32_t* launched) {
     q.op = r.op;
     q.wait = wait;
     q.stage = (unsigned)stage;
-    if (wait == -2) {
-      // same wait as the first request of this stage
-      for (int j = (int)nreq - 1; j >= 0; --j)
-        if (sl->h_reqs[j].stage == (unsigned)stage && sl->h_reqs[j].wait != -2) {
-          q.wait = sl->h_reqs[j].wait;
-          break;
-        }
-    }
     sl->h_reqs[nreq] = q;
     order.push_back({stage_depth[stage], nreq});
     sl->tags.push_back(r.tag);
@@ -603,7 +596,10 @@ static hx_status server_step(hx_server* sv, uint32_t* launched) {
   sv->st.requests += nreq;
   sv->st.keys += round_keys;
   sv->st.max_stage_depth = std::max<uint32_t>(sv->st.max_stage_depth, (uint32_t)max_depth);
-  for (auto& x : sl->inserts) sv->maps[x.first].in_flight += x.second;
+  for (auto& x : sl->inserts) {
+    sv->maps[x.first].in_flight += x.second;
+    sv->maps[x.first].fill_ub += x.second;  // counted from launch until a snapshot covers it
+  }
   for (auto& x : sl->erases) {
     sv->maps[x.first].in_flight_erase += x.second;
     sv->maps[x.first].tomb_ub += x.second;
