@@ -1,0 +1,409 @@
+/*
+ * hashinator_compat.h — drop-in C++ surface of Hashinator's accelerated API
+ * over libhx (hx.h). Compile the including translation unit with nvcc and
+ * link libhx.so.
+ *
+ *   Hashinator::Hashmap<K,V>      hashinator/hashinator.h:59-62  (K = V = uint32_t or uint64_t)
+ *   Hashinator::hash_pair<K,V>    hashinator/hash_pair.h:30-75
+ *   Hashinator::Info / status     hashinator/defaults.h:44-54, common.h:85
+ *   split::SplitVector<T>         splitvector/splitvec.h:83 (managed memory, minimal surface)
+ *   split::tools::copy_if         splitvector/split_tools.h:1129-1223
+ *   split::tools::split_prefix_scan  split_tools.h:363-418
+ *
+ * Behaviour matches the reference's: every accelerated call blocks the host
+ * until its stream is done (hashinator/hashers.h:55 and siblings), CUDA
+ * errors abort with a message (splitvector/split_allocators.h:33-40), and a
+ * full table is reported through peek_status() == status::fail. Rules are
+ * either hx_pred descriptors (run inside libhx) or any __host__ __device__
+ * functor bool(T&) (run by the header's kernels in this translation unit,
+ * with offsets from libhx's scan).
+ */
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <limits>
+#include <type_traits>
+
+#include "hx.h"
+
+namespace hxcompat {
+inline void check(hx_status st, const char* what) {
+  if (st != HX_OK) {
+    std::fprintf(stderr, "hashinator_compat: %s failed: %s (cuda error %d)\n", what, hx_status_string(st),
+                 hx_last_cuda_error());
+    std::abort();
+  }
+}
+inline void check_cuda(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    std::fprintf(stderr, "hashinator_compat: %s failed: %s\n", what, cudaGetErrorString(e));
+    std::abort();
+  }
+}
+}  // namespace hxcompat
+
+namespace Hashinator {
+
+enum status { success, fail, invalid };
+enum targets { host, device, automatic };
+
+template <typename T, typename U>
+struct hash_pair {
+  T first;
+  U second;
+  __host__ __device__ hash_pair() : first(T()), second(U()) {}
+  __host__ __device__ hash_pair(const T& f, const U& s) : first(f), second(s) {}
+  __host__ __device__ bool operator==(const hash_pair& y) const { return first == y.first && second == y.second; }
+  __host__ __device__ bool operator!=(const hash_pair& y) const { return !(*this == y); }
+};
+template <class T, class U>
+__host__ __device__ inline hash_pair<T, U> make_pair(T x, U y) {
+  return hash_pair<T, U>(x, y);
+}
+
+struct Info {
+  int sizePower;
+  size_t fill;
+  size_t currentMaxBucketOverflow;
+  size_t tombstoneCounter;
+  status err;
+};
+
+}  // namespace Hashinator
+
+namespace split {
+
+/* Managed-memory vector (the reference's default allocator is
+ * cudaMallocManaged, split_allocators.h:62-129), with the subset of the
+ * SplitVector surface the accelerated API and its tests use. */
+template <typename T>
+class SplitVector {
+  T* d_ = nullptr;
+  size_t size_ = 0, cap_ = 0;
+
+  void reallocate(size_t cap) {
+    T* p = nullptr;
+    if (cap) hxcompat::check_cuda(cudaMallocManaged(&p, cap * sizeof(T)), "cudaMallocManaged");
+    if (d_) {
+      hxcompat::check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+      for (size_t i = 0; i < size_ && i < cap; ++i) p[i] = d_[i];
+      cudaFree(d_);
+    }
+    d_ = p;
+    cap_ = cap;
+  }
+
+ public:
+  using value_type = T;
+  using iterator = T*;
+  using const_iterator = const T*;
+  SplitVector() = default;
+  explicit SplitVector(size_t n) { resize(n); }
+  SplitVector(size_t n, const T& v) {
+    resize(n);
+    for (size_t i = 0; i < n; ++i) d_[i] = v;
+  }
+  SplitVector(const SplitVector& o) {
+    reserve(o.size_);
+    hxcompat::check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    for (size_t i = 0; i < o.size_; ++i) d_[i] = o.d_[i];
+    size_ = o.size_;
+  }
+  SplitVector& operator=(const SplitVector& o) {
+    if (this != &o) {
+      resize(o.size_);
+      hxcompat::check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+      for (size_t i = 0; i < o.size_; ++i) d_[i] = o.d_[i];
+    }
+    return *this;
+  }
+  ~SplitVector() {
+    if (d_) cudaFree(d_);
+  }
+  T* data() { return d_; }
+  const T* data() const { return d_; }
+  size_t size() const { return size_; }
+  size_t capacity() const { return cap_; }
+  bool empty() const { return size_ == 0; }
+  void reserve(size_t n) {
+    if (n > cap_) reallocate(n);
+  }
+  void resize(size_t n, bool /*eco*/ = false) {
+    reserve(n);
+    size_ = n;
+  }
+  void clear() { size_ = 0; }
+  void push_back(const T& v) {
+    if (size_ == cap_) reallocate(cap_ ? 2 * cap_ : 8);
+    d_[size_++] = v;
+  }
+  T& operator[](size_t i) { return d_[i]; }
+  const T& operator[](size_t i) const { return d_[i]; }
+  T& at(size_t i) { return d_[i]; }
+  T* begin() { return d_; }
+  T* end() { return d_ + size_; }
+  const T* begin() const { return d_; }
+  const T* end() const { return d_ + size_; }
+  void erase(T* first, T* last) {  // erase(range) (splitvec.h:1499): only the tail form is used
+    if (last == end()) size_ = (size_t)(first - d_);
+  }
+  void optimizeGPU(cudaStream_t = 0) {}
+  void optimizeCPU(cudaStream_t = 0) {}
+};
+
+namespace tools {
+namespace detail {
+
+template <typename T, typename Rule>
+__global__ void count_tiles(const T* in, size_t n, Rule rule, uint32_t* counts) {
+  __shared__ uint32_t s;
+  if (threadIdx.x == 0) s = 0;
+  __syncthreads();
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  bool sel = false;
+  if (i < n) {
+    T x = in[i];
+    sel = rule(x);
+  }
+  const unsigned b = __ballot_sync(0xffffffffu, sel);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(&s, (uint32_t)__popc(b));
+  __syncthreads();
+  if (threadIdx.x == 0) counts[blockIdx.x] = s;
+}
+
+template <typename T, typename Rule>
+__global__ void scatter_tiles(const T* in, size_t n, Rule rule, const uint32_t* offsets, T* out, size_t cap,
+                              unsigned long long* total, size_t nblocks) {
+  __shared__ uint32_t warp_base[32];
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  bool sel = false;
+  T x;
+  if (i < n) {
+    x = in[i];
+    sel = rule(x);
+  }
+  const unsigned b = __ballot_sync(0xffffffffu, sel);
+  if (lane == 0) warp_base[warp] = __popc(b);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t acc = 0;
+    for (unsigned w = 0; w < blockDim.x / 32; ++w) {
+      const uint32_t c = warp_base[w];
+      warp_base[w] = acc;
+      acc += c;
+    }
+    if (blockIdx.x == nblocks - 1) *total = (unsigned long long)offsets[blockIdx.x] + acc;
+  }
+  __syncthreads();
+  if (sel) {
+    const size_t dst = (size_t)offsets[blockIdx.x] + warp_base[warp] + __popc(b & ((1u << lane) - 1u));
+    if (dst < cap) out[dst] = x;
+  }
+}
+
+// Stable compaction with a user functor: per-block counts, libhx exclusive
+// scan of the counts, order-preserving scatter.
+template <typename T, typename Rule>
+size_t copy_if_functor(const T* in, T* out, size_t n, size_t cap, Rule rule, cudaStream_t s) {
+  if (n == 0) return 0;
+  const unsigned block = 256;
+  const size_t nb = (n + block - 1) / block;
+  uint32_t* counts = nullptr;
+  unsigned long long* total = nullptr;
+  hxcompat::check_cuda(cudaMallocAsync(&counts, 2 * nb * sizeof(uint32_t) + 16, s), "cudaMallocAsync");
+  uint32_t* offsets = counts + nb;
+  total = reinterpret_cast<unsigned long long*>(counts + 2 * nb);  // 8-byte aligned: 2*nb words
+  count_tiles<<<(unsigned)nb, block, 0, s>>>(in, n, rule, counts);
+  hxcompat::check(hx_exclusive_scan_u32(counts, offsets, nb, nullptr, 0, s), "hx_exclusive_scan_u32");
+  scatter_tiles<<<(unsigned)nb, block, 0, s>>>(in, n, rule, offsets, out, cap, total, nb);
+  unsigned long long h = 0;
+  hxcompat::check_cuda(cudaMemcpyAsync(&h, total, sizeof(h), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+  hxcompat::check_cuda(cudaFreeAsync(counts, s), "cudaFreeAsync");
+  hxcompat::check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  return (size_t)h;
+}
+
+template <typename T>
+constexpr int elem_bytes() {
+  return (int)sizeof(T);
+}
+
+}  // namespace detail
+
+/* copy_if(in, out, rule, stream) (split_tools.h:1129): out gets the selected
+ * elements in order and is resized to their count. */
+template <typename T, typename Rule>
+void copy_if(SplitVector<T>& input, SplitVector<T>& output, Rule rule, cudaStream_t s = 0) {
+  size_t c;
+  if constexpr (std::is_same<Rule, hx_pred>::value) {
+    uint64_t h = 0;
+    const hx_status st = hx_copy_if(input.data(), output.data(), input.size(), detail::elem_bytes<T>(), &rule,
+                                    output.size(), nullptr, &h, nullptr, 0, s);
+    if (st != HX_OK && st != HX_ERR_CAPACITY) hxcompat::check(st, "hx_copy_if");
+    c = (size_t)h;
+  } else {
+    c = detail::copy_if_functor(input.data(), output.data(), input.size(), output.size(), rule, s);
+  }
+  output.erase(output.data() + (c < output.size() ? c : output.size()), output.end());
+}
+
+/* copy_if(T* in, T* out, size, rule, stack, max_size, stream)
+ * (split_tools.h:1211): returns the count. */
+template <typename T, typename Rule>
+size_t copy_if(T* input, T* output, size_t size, Rule rule, void* /*stack*/, size_t /*max_size*/, cudaStream_t s = 0) {
+  return detail::copy_if_functor(input, output, size, size, rule, s);
+}
+
+/* split_prefix_scan(in, out, stream) (split_tools.h:363): exclusive sum of
+ * uint32_t, any length (the reference asserts a power of two). */
+inline void split_prefix_scan(SplitVector<uint32_t>& input, SplitVector<uint32_t>& output, cudaStream_t s = 0) {
+  output.resize(input.size());
+  hxcompat::check(hx_exclusive_scan_u32(input.data(), output.data(), input.size(), nullptr, 0, s),
+                  "hx_exclusive_scan_u32");
+  hxcompat::check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+}
+
+}  // namespace tools
+}  // namespace split
+
+namespace Hashinator {
+
+template <typename KEY_TYPE, typename VAL_TYPE, KEY_TYPE EMPTYBUCKET = std::numeric_limits<KEY_TYPE>::max(),
+          KEY_TYPE TOMBSTONE = EMPTYBUCKET - 1>
+class Hashmap {
+  static_assert(std::is_same<KEY_TYPE, VAL_TYPE>::value &&
+                    (std::is_same<KEY_TYPE, uint32_t>::value || std::is_same<KEY_TYPE, uint64_t>::value),
+                "libhx serves hash_pair<uint32_t,uint32_t> and hash_pair<uint64_t,uint64_t>");
+  static_assert(EMPTYBUCKET == std::numeric_limits<KEY_TYPE>::max() && TOMBSTONE == EMPTYBUCKET - 1,
+                "libhx uses the reference's default sentinels");
+  using pair_t = hash_pair<KEY_TYPE, VAL_TYPE>;
+  hx_map* m_ = nullptr;
+
+  void sync(cudaStream_t s) const { hxcompat::check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize"); }
+  hx_info info(cudaStream_t s = 0) const {
+    hx_info i;
+    hxcompat::check(hx_get_info(m_, &i, s), "hx_get_info");
+    return i;
+  }
+
+ public:
+  Hashmap() : Hashmap(5) {}  // Hashmap() starts at size power 5 (hashinator.h:109-118)
+  explicit Hashmap(int sizepower) {
+    hxcompat::check(hx_map_create(&m_, (int)sizeof(KEY_TYPE), (int)sizeof(VAL_TYPE), sizepower, nullptr),
+                    "hx_map_create");
+  }
+  Hashmap(const Hashmap&) = delete;
+  Hashmap& operator=(const Hashmap&) = delete;
+  ~Hashmap() {
+    if (m_) hx_map_destroy(m_);
+  }
+
+  // ---- accelerated API (hashinator.h:1262-1409) ----
+  template <bool prefetches = true>
+  void insert(KEY_TYPE* keys, VAL_TYPE* vals, size_t len, float targetLF = 0.5, cudaStream_t s = 0) {
+    hxcompat::check(hx_insert(m_, keys, vals, len, targetLF, s), "hx_insert");
+    sync(s);
+  }
+  template <bool prefetches = true>
+  void insert(pair_t* src, size_t len, float targetLF = 0.5, cudaStream_t s = 0) {
+    hxcompat::check(hx_insert_pairs(m_, src, len, targetLF, s), "hx_insert_pairs");
+    sync(s);
+  }
+  template <bool prefetches = true>
+  void retrieve(KEY_TYPE* keys, VAL_TYPE* vals, size_t len, cudaStream_t s = 0) {
+    hxcompat::check(hx_retrieve(m_, keys, vals, len, s), "hx_retrieve");
+    sync(s);
+  }
+  template <bool prefetches = true>
+  void retrieve(pair_t* src, size_t len, cudaStream_t s = 0) {
+    hxcompat::check(hx_retrieve_pairs(m_, src, len, s), "hx_retrieve_pairs");
+    sync(s);
+  }
+  template <bool prefetches = true>
+  void erase(KEY_TYPE* keys, size_t len, cudaStream_t s = 0) {
+    hxcompat::check(hx_erase(m_, keys, len, s), "hx_erase");
+    sync(s);
+  }
+  template <bool prefetches = true>
+  void clean_tombstones(cudaStream_t s = 0) {
+    hxcompat::check(hx_clean_tombstones(m_, s), "hx_clean_tombstones");
+    sync(s);
+  }
+  template <bool prefetches = true>
+  void device_rehash(int newSizePower, cudaStream_t s = 0) {
+    hxcompat::check(hx_resize(m_, newSizePower, s), "hx_resize");
+    sync(s);
+  }
+  void resize(int newSizePower, targets = targets::device, cudaStream_t s = 0) { device_rehash(newSizePower, s); }
+  template <bool prefetches = true>
+  void clear(targets = targets::device, cudaStream_t s = 0, size_t = 0) {
+    hxcompat::check(hx_clear(m_, s), "hx_clear");
+    sync(s);
+  }
+
+  /* extractPattern(hash_pair*, Rule, stream) (hashinator.h:1168): bucket
+   * order; the output must hold the result. */
+  template <typename Rule>
+  size_t extractPattern(pair_t* elements, Rule rule, cudaStream_t s = 0) {
+    void* b = nullptr;
+    uint64_t nb = 0;
+    hxcompat::check(hx_bucket_data(m_, &b, &nb), "hx_bucket_data");
+    if constexpr (std::is_same<Rule, hx_pred>::value) {
+      uint64_t c = 0;
+      const hx_status st = hx_extract_pattern(m_, &rule, elements, nb, nullptr, &c, s);
+      if (st != HX_OK && st != HX_ERR_CAPACITY) hxcompat::check(st, "hx_extract_pattern");
+      return (size_t)c;
+    } else {
+      return split::tools::detail::copy_if_functor(static_cast<pair_t*>(b), elements, nb, nb, rule, s);
+    }
+  }
+  /* extractPattern(SplitVector&, Rule, stream) (hashinator.h:1155): resized
+   * to the count. */
+  template <bool prefetches = true, typename Rule>
+  size_t extractPattern(split::SplitVector<pair_t>& elements, Rule rule, cudaStream_t s = 0) {
+    void* b = nullptr;
+    uint64_t nb = 0;
+    hxcompat::check(hx_bucket_data(m_, &b, &nb), "hx_bucket_data");
+    elements.resize(nb);
+    const size_t c = extractPattern(elements.data(), rule, s);
+    elements.erase(elements.data() + c, elements.end());
+    return c;
+  }
+
+  // ---- metadata (hashinator.h:434-457, 611, 228) ----
+  status peek_status() {
+    int32_t v = 0;
+    hxcompat::check(hx_peek_status(m_, &v, nullptr), "hx_peek_status");
+    return static_cast<status>(v);
+  }
+  int getSizePower() const { return info().size_power; }
+  size_t size() const { return info().fill; }
+  size_t bucket_count() const { return info().bucket_count; }
+  size_t tombstone_count() const { return info().tombstone_counter; }
+  float load_factor() const {
+    const hx_info i = info();
+    return (float)i.fill / (float)i.bucket_count;
+  }
+  constexpr KEY_TYPE get_emptybucket() const { return EMPTYBUCKET; }
+  constexpr KEY_TYPE get_tombstone() const { return TOMBSTONE; }
+  void copyMetadata(Info* dst, cudaStream_t s = 0) {
+    const hx_info i = info(s);
+    *dst = Info{i.size_power, i.fill, i.current_max_bucket_overflow, i.tombstone_counter,
+                static_cast<status>(i.err)};
+  }
+  template <bool warn = true>
+  pair_t* expose_bucketdata() {
+    void* b = nullptr;
+    hxcompat::check(hx_bucket_data(m_, &b, nullptr), "hx_bucket_data");
+    return static_cast<pair_t*>(b);
+  }
+  void optimizeGPU(cudaStream_t = 0) {}
+  void optimizeCPU(cudaStream_t = 0) {}
+  hx_map* handle() { return m_; }
+};
+
+}  // namespace Hashinator
