@@ -268,6 +268,140 @@ def run_serving(args, dev):
             "latency": "arrival (host clock) to the end of the request's round (CUDA event on the serving stream)"}
 
 
+def _ev_time(stream, fn, reps=3):
+    import torch
+    ts = []
+    for r in range(reps + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if r:
+            ts.append(e0.elapsed_time(e1) / 1e3)
+    return float(np.median(ts))
+
+
+def run_lf_sweep(args, stream, dev, peak):
+    """The large single map: u32 and u64 keys, 2^27 buckets, LF 0.5/0.75/0.9 (key count adjusted):
+    insert, 50/50 query, erase 30%, clean_tombstones, re-query. Each op timed alone with CUDA events
+    on a fresh table (insert) or the state the sequence reaches."""
+    import torch
+    import hashinator_gb300 as hx
+    from hashinator_gb300 import workloads
+    sp = 27
+    out = []
+    for width in (4, 8):
+        sig = np.int32 if width == 4 else np.int64
+        nmax = int(0.9 * (1 << sp))
+        keys, vals, q, er = workloads.large_map_workload(nmax, width, 31 + width)
+
+        def dev_t(a):
+            return torch.from_numpy(np.ascontiguousarray(a).view(sig)).to(dev)
+
+        dk, dv = dev_t(keys), dev_t(vals)
+        ib, qb, eb = {4: 72, 8: 80}[width], {4: 40, 8: 48}[width], {4: 68, 8: 72}[width]
+        for lf in (0.5, 0.75, 0.9):
+            n = int(lf * (1 << sp))
+            rng = np.random.default_rng(int(lf * 100) + width)
+            # queries: half hits among the first n keys, half absent keys, shuffled
+            hsel = workloads.affine_sample(n, n // 2, rng)
+            miss = workloads.distinct_keys(n - n // 2, width, 31 + width, offset=nmax + 4096)
+            fill = np.iinfo(keys.dtype).max - 7
+            perm = workloads.affine_sample(n, n, rng)
+            qq = np.concatenate([keys[hsel], miss])[perm]
+            expect = np.concatenate([vals[hsel], np.full(len(miss), fill, keys.dtype)])[perm]
+            ee = keys[workloads.affine_sample(n, int(0.3 * n), rng)]
+            dq, de = dev_t(qq), dev_t(ee)
+            o = dev_t(np.full(n, fill, keys.dtype))
+            m = hx.Hashmap(sp, width, stream=stream)
+            t_ins = _ev_time(stream, lambda: (m.clear(stream=stream), m.insert(dk[:n], dv[:n], target_lf=0.0,
+                                                                                 stream=stream)))
+            t_clear = _ev_time(stream, lambda: m.clear(stream=stream))
+            t_ins -= t_clear
+            m.clear(stream=stream)
+            m.insert(dk[:n], dv[:n], target_lf=0.0, stream=stream)
+            t_q = _ev_time(stream, lambda: m.retrieve(dq, o, stream=stream))
+            got = o[:65536].cpu().numpy().view(keys.dtype)
+            exact = bool(np.array_equal(got, expect[:65536]))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            m.erase(de, stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t_e = e0.elapsed_time(e1) / 1e3
+            e0.record(stream)
+            m.clean_tombstones(stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t_c = e0.elapsed_time(e1) / 1e3
+            inf = m.info(stream=stream)
+            t_q2 = _ev_time(stream, lambda: m.retrieve(dq, o, stream=stream))
+            pb = 8 if width == 4 else 16
+            out.append({"key_bytes": width, "load_factor": lf, "keys": n,
+                        "insert_Mkeys_s": round(n / t_ins / 1e6, 1), "insert_frac": round(n * ib / t_ins / 1e9 / peak, 4),
+                        "query_Mkeys_s": round(n / t_q / 1e6, 1), "query_frac": round(n * qb / t_q / 1e9 / peak, 4),
+                        "erase_Mkeys_s": round(len(ee) / t_e / 1e6, 1),
+                        "erase_frac": round(len(ee) * eb / t_e / 1e9 / peak, 4),
+                        "clean_ms": round(t_c * 1e3, 3),
+                        "clean_scan_GB_s": round((1 << sp) * pb / t_c / 1e9, 1),
+                        "requery_Mkeys_s": round(n / t_q2 / 1e6, 1),
+                        "fill_after": int(inf.fill), "tombstones_after_clean": int(inf.tombstone_counter),
+                        "fill_ok": int(inf.fill) == n - len(ee), "query_sample_exact": exact})
+            m.close()
+            del dq, de, o
+        del dk, dv
+        torch.cuda.empty_cache()
+    return {"note": "fraction of the measured HBM copy bandwidth for algorithmic bytes (insert 72/80, query 40/48, "
+                    "erase 68/72 B per key); clean_tombstones includes the scan of the whole table",
+            "runs": out}
+
+
+def run_streaming(args, stream, dev, peak):
+    """copy_if on 2^28 u32 with (x % 100) < s, s = 1/50/99; exclusive scan of 2^28 u32 in [0, 16);
+    extractPattern (value even, valid keys) on the 2^26-key u32 map of 2^27 buckets."""
+    import torch
+    import hashinator_gb300 as hx
+    from hashinator_gb300 import workloads
+    n = 1 << 28
+    x = torch.randint(0, 2**31 - 1, (n,), dtype=torch.int64, device=dev, generator=torch.Generator(device=dev).manual_seed(7))
+    x = (x * 2 + (x >> 17 & 1)).to(torch.int32)  # uniform over the 32-bit range, as int32 bits
+    out = torch.empty_like(x)
+    res = {}
+    for s_ in (1, 50, 99):
+        c = hx.tools.copy_if(x, out, hx.Pred.mod_lt(100, s_))
+        nb = hx.tools.scratch_bytes(hx.SCRATCH_COPY_IF, n)
+        scratch = torch.empty(nb, dtype=torch.uint8, device=dev)
+        dc = torch.zeros(1, dtype=torch.int64, device=dev)
+        t = _ev_time(stream, lambda: hx.tools.copy_if(x, out, hx.Pred.mod_lt(100, s_), scratch=scratch,
+                                                      scratch_bytes=nb, stream=stream, d_count=dc))
+        res[f"copy_if_s{s_}"] = {"selected": int(c), "ms": round(t * 1e3, 3),
+                                 "GB_s": round((4 * n + 4 * c) / t / 1e9, 1),
+                                 "frac": round((4 * n + 4 * c) / t / 1e9 / peak, 4)}
+    y = (x & 15).contiguous()
+    nb = hx.tools.scratch_bytes(hx.SCRATCH_SCAN, n)
+    scratch = torch.empty(nb, dtype=torch.uint8, device=dev)
+    t = _ev_time(stream, lambda: hx.tools.split_prefix_scan(y, out, scratch=scratch, scratch_bytes=nb, stream=stream))
+    res["exclusive_scan"] = {"ms": round(t * 1e3, 3), "GB_s": round(8 * n / t / 1e9, 1),
+                             "frac": round(8 * n / t / 1e9 / peak, 4)}
+    del x, y, out, scratch
+    keys, vals, _, _ = workloads.map_workload(1 << 26, 4, 2026, erase_frac=0.0)
+    m = hx.Hashmap(27, 4, stream=stream)
+    m.insert(torch.from_numpy(keys.view(np.int32)).to(dev), torch.from_numpy(vals.view(np.int32)).to(dev),
+             target_lf=0.0, stream=stream)
+    ex = torch.empty(2 * (1 << 26), dtype=torch.int32, device=dev)
+    c = m.extract_pattern(hx.Pred.value_even(), ex, capacity=1 << 26, stream=stream)
+    dc = torch.zeros(1, dtype=torch.int64, device=dev)
+    t = _ev_time(stream, lambda: m.extract_pattern(hx.Pred.value_even(), ex, capacity=1 << 26, stream=stream,
+                                                   d_count=dc))
+    byts = 8 * (1 << 27) + 8 * c
+    res["extract_pattern_value_even"] = {"selected": int(c), "expected": int((vals % 2 == 0).sum()),
+                                         "ms": round(t * 1e3, 3), "GB_s": round(byts / t / 1e9, 1),
+                                         "frac": round(byts / t / 1e9 / peak, 4)}
+    m.close()
+    return res
+
+
 def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -498,6 +632,10 @@ def run_ours(args):
     serving = None
     if not args.no_serving:
         serving = run_serving(args, dev)
+    lf_sweep = streaming = None
+    if not args.no_extra:
+        lf_sweep = run_lf_sweep(args, stream, dev, peak)
+        streaming = run_streaming(args, stream, dev, peak)
 
     if rank == 0:
         metric = METRIC if args.log_keys == 26 else METRIC.replace("2^26 keys, 2^27", f"2^{args.log_keys} keys, 2^{sp}")
@@ -511,7 +649,7 @@ def run_ours(args):
                            "l2": "inputs larger than L2 (1 GiB table, 256 MiB arrays); no flush",
                            "group_width": args.group or "default"},
                 "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
-                "batched": batched, "serving": serving,
+                "batched": batched, "serving": serving, "large_map_lf_sweep": lf_sweep, "streaming": streaming,
                 "clocks": clocks}
         print(json.dumps(line), flush=True)
     m.close()
@@ -533,6 +671,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-maps", type=int, default=4096)
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the LF sweep and the streaming primitives")
     ap.add_argument("--serving-maps", type=int, default=1024)
     ap.add_argument("--serving-requests", type=int, default=20000)
     ap.add_argument("--serving-rates", type=float, nargs="+", default=[2.5e5, 5e5, 1e6, 2e6, 4e6])

@@ -240,3 +240,35 @@ def serving_trace(n_maps: int, n_requests: int, seed: int, init_log=(8.0, 20.0),
             "req_map": req_map.astype(np.uint32), "req_op": req_op.astype(np.uint32), "req_n": req_n,
             "req_offsets": req_off, "req_keys": keys_of(req_pos), "req_vals": values(len(req_pos), width, seed + 12),
             "arrival_ns": arrival}
+
+
+def affine_sample(n: int, k: int, rng) -> np.ndarray:
+    """k distinct indices in [0, n) (k <= n) from a random affine permutation, O(k)."""
+    import math
+    if k == 0 or n == 0:
+        return np.zeros(0, np.int64)
+    while True:
+        a = int(rng.integers(1, max(n, 2)))
+        if math.gcd(a, n) == 1:
+            break
+    b = int(rng.integers(0, n))
+    j = np.arange(k, dtype=np.int64)
+    return (a * j + b) % n
+
+
+def large_map_workload(n: int, width: int, seed: int, hit_frac: float = 0.5, erase_frac: float = 0.3):
+    """map_workload for very large n without O(n log n) sampling: hits and the
+    erase set are affine samples of the inserted keys, the query order an
+    affine shuffle."""
+    rng = np.random.default_rng(seed + 1)
+    keys = distinct_keys(n, width, seed)
+    vals = values(n, width, seed)
+    n_hit = int(round(n * hit_frac))
+    hits = keys[affine_sample(n, n_hit, rng)]
+    misses = distinct_keys(n - n_hit, width, seed, offset=n + 64)
+    q = np.empty(n, keys.dtype)
+    pos = affine_sample(n, n, rng)
+    q[pos[:n_hit]] = hits
+    q[pos[n_hit:]] = misses
+    erase = keys[affine_sample(n, int(round(n * erase_frac)), rng)]
+    return keys, vals, q, erase
