@@ -124,10 +124,8 @@ class ClockSampler:
 
 
 def dist_setup():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from hashinator_gb300.dist import env_ranks
+    return env_ranks()
 
 
 def cpu_baseline(width: int = 4, log_n: int = 24):
@@ -451,7 +449,8 @@ def run_ours(args):
     width = 4
     n = 1 << args.log_keys
     sp = args.log_keys + 1
-    keys, vals, q, _ = workloads.map_workload(n, width, 2026 + rank, erase_frac=0.0)
+    from hashinator_gb300.dist import max_over_ranks, replica_seed
+    keys, vals, q, _ = workloads.map_workload(n, width, replica_seed(2026, rank), erase_frac=0.0)
 
     def to_dev(a):
         return torch.from_numpy(a.view(np.int32)).to(dev)
@@ -498,11 +497,7 @@ def run_ours(args):
     stop.record(stream)
     torch.cuda.synchronize()
     launches = hx.kernel_launch_count() - l0
-    elapsed = start.elapsed_time(stop) / 1e3
-    if world > 1:
-        t = torch.tensor([elapsed], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = max_over_ranks(start.elapsed_time(stop) / 1e3, dev)
     clocks = sampler.stop()
     t_clear = float(np.mean([e[0].elapsed_time(e[1]) for e in evs])) / 1e3
     t_ins = float(np.mean([e[1].elapsed_time(e[2]) for e in evs])) / 1e3
@@ -568,11 +563,7 @@ def run_ours(args):
             e2e_step()
         s1.record(stream)
         torch.cuda.synchronize()
-        e_el = s0.elapsed_time(s1) / 1e3
-        if world > 1:
-            t = torch.tensor([e_el], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e_el = float(t.item())
+        e_el = max_over_ranks(s0.elapsed_time(s1) / 1e3, dev)
         # the e2e results equal the device-timed results
         assert np.array_equal(h_out.numpy().view(np.uint32), host_out)
         e2e = {"value": round(world * 2 * n * args.steps / e_el / 1e6, 3), "unit": "Mkeys/s",

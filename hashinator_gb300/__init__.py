@@ -112,6 +112,9 @@ _SIGS = {
     "hx_clean_tombstones": [ctypes.c_void_p, ctypes.c_void_p],
     "hx_extract_pattern": [ctypes.c_void_p, ctypes.POINTER(_CPred), ctypes.c_void_p, ctypes.c_uint64,
                            ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.c_void_p],
+    "hx_extract_keys": [ctypes.c_void_p, ctypes.POINTER(_CPred), ctypes.c_void_p, ctypes.c_uint64,
+                        ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.c_void_p],
+    "hx_map_device_view": [ctypes.c_void_p, ctypes.c_void_p],
     "hx_resize": [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p],
     "hx_clear": [ctypes.c_void_p, ctypes.c_void_p],
     "hx_get_info": [ctypes.c_void_p, ctypes.POINTER(Info), ctypes.c_void_p],
@@ -342,6 +345,27 @@ class Hashmap:
         if st not in (HX_OK, HX_ERR_CAPACITY):
             _check(st, "hx_extract_pattern")
         return cnt.value
+
+    def extract_keys_by_pattern(self, pred: Pred, out, capacity: int | None = None, stream=None,
+                                d_count=None) -> int:
+        """extractKeysByPattern(keys, rule): the keys of the buckets where the
+        rule holds, in bucket order; count as for extract_pattern."""
+        cap = _numel(out) if capacity is None else capacity
+        cp = pred.c()
+        if d_count is not None:
+            _check(self._h.hx_extract_keys(self._m, ctypes.byref(cp), _ptr(out), cap, _ptr(d_count), None,
+                                           _stream(stream)), "hx_extract_keys")
+            return -1
+        cnt = ctypes.c_uint64()
+        st = self._h.hx_extract_keys(self._m, ctypes.byref(cp), _ptr(out), cap, None, ctypes.byref(cnt),
+                                     _stream(stream))
+        if st not in (HX_OK, HX_ERR_CAPACITY):
+            _check(st, "hx_extract_keys")
+        return cnt.value
+
+    def extract_all_keys(self, out, capacity: int | None = None, stream=None) -> int:
+        """extractAllKeys(keys): every valid key, in bucket order."""
+        return self.extract_keys_by_pattern(Pred.valid_key(), out, capacity, stream)
 
     def resize(self, new_size_power: int, stream=None) -> None:
         _check(self._h.hx_resize(self._m, new_size_power, _stream(stream)), "hx_resize")

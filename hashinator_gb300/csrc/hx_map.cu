@@ -722,6 +722,52 @@ hx_status map_find_view(hx_map* m, const void* keys, void* vals, void* pairs, ui
 
 using namespace hx;
 
+// extractPattern (KEYS = false) and extractKeysByPattern (KEYS = true): one
+// order-preserving compaction pass over the bucket array.
+template <bool KEYS>
+static hx_status extract(hx_map* m, const hx_pred* pred, void* d_out, uint64_t capacity, uint64_t* d_count,
+                         uint64_t* h_count, hx_stream stream) {
+  if (!valid_map(m) || !pred) return HX_ERR_INVALID_ARG;
+  if (pred->op > HX_PRED_NOT_HOME || (pred->op == HX_PRED_MOD_LT && pred->a == 0)) return HX_ERR_INVALID_ARG;
+  if (capacity && !d_out) return HX_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::lock_guard<std::mutex> g(m->mu);
+  const uint64_t n = nslots(m);
+  const bool p32 = is_p32(m);
+  const uint64_t tiles = p32 ? compact_tiles<P32>(n) : compact_tiles<P64>(n);
+  const uint64_t sc_bytes = (scan_scratch_bytes(tiles) + 255) / 256 * 256;
+  hx_status st = ensure_scratch(m, sc_bytes + 256, s);
+  if (st != HX_OK) return st;
+  unsigned long long* cnt = d_count ? reinterpret_cast<unsigned long long*>(d_count)
+                                    : reinterpret_cast<unsigned long long*>(static_cast<char*>(m->scratch) + sc_bytes);
+  cudaError_t e;
+  CleanArgs cl{nullptr, nullptr};
+  if (p32) {
+    using O = typename std::conditional<KEYS, uint32_t, P32>::type;
+    e = launch_compact<P32, false, O>(static_cast<const P32*>(m->buckets), static_cast<O*>(d_out), n, *pred,
+                                      TableRef<P32>{static_cast<const P32*>(m->buckets), m->sp}, capacity, cnt,
+                                      m->scratch, cl, s);
+  } else {
+    using O = typename std::conditional<KEYS, uint64_t, P64>::type;
+    e = launch_compact<P64, false, O>(static_cast<const P64*>(m->buckets), static_cast<O*>(d_out), n, *pred,
+                                      TableRef<P64>{static_cast<const P64*>(m->buckets), m->sp}, capacity, cnt,
+                                      m->scratch, cl, s);
+  }
+  if (e != cudaSuccess) return cuda_status(e);
+  if ((st = after_launch()) != HX_OK) return st;
+  if (h_count) {
+    unsigned long long c = 0;
+    unsigned int err = 0;
+    HX_CUDA(cudaMemcpyAsync(&c, cnt, sizeof(c), cudaMemcpyDeviceToHost, s));
+    HX_CUDA(cudaMemcpyAsync(&err, static_cast<char*>(m->scratch) + 4, sizeof(err), cudaMemcpyDeviceToHost, s));
+    HX_CUDA(cudaStreamSynchronize(s));
+    *h_count = c;
+    if (err) return HX_ERR_TIMEOUT;
+    if (c > capacity) return HX_ERR_CAPACITY;
+  }
+  return HX_OK;
+}
+
 extern "C" {
 
 hx_status hx_map_create(hx_map** out, int key_bytes, int val_bytes, int size_power, hx_stream stream) {
@@ -862,43 +908,12 @@ hx_status hx_clean_tombstones(hx_map* m, hx_stream stream) {
 
 hx_status hx_extract_pattern(hx_map* m, const hx_pred* pred, void* d_out, uint64_t capacity, uint64_t* d_count,
                              uint64_t* h_count, hx_stream stream) {
-  if (!valid_map(m) || !pred) return HX_ERR_INVALID_ARG;
-  if (pred->op > HX_PRED_NOT_HOME || (pred->op == HX_PRED_MOD_LT && pred->a == 0)) return HX_ERR_INVALID_ARG;
-  if (capacity && !d_out) return HX_ERR_INVALID_ARG;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  std::lock_guard<std::mutex> g(m->mu);
-  const uint64_t n = nslots(m);
-  const bool p32 = is_p32(m);
-  const uint64_t tiles = p32 ? compact_tiles<P32>(n) : compact_tiles<P64>(n);
-  const uint64_t sc_bytes = (scan_scratch_bytes(tiles) + 255) / 256 * 256;
-  hx_status st = ensure_scratch(m, sc_bytes + 256, s);
-  if (st != HX_OK) return st;
-  unsigned long long* cnt = d_count ? reinterpret_cast<unsigned long long*>(d_count)
-                                    : reinterpret_cast<unsigned long long*>(static_cast<char*>(m->scratch) + sc_bytes);
-  cudaError_t e;
-  CleanArgs cl{nullptr, nullptr};
-  if (p32) {
-    e = launch_compact<P32, false>(static_cast<const P32*>(m->buckets), static_cast<P32*>(d_out), n, *pred,
-                                   TableRef<P32>{static_cast<const P32*>(m->buckets), m->sp}, capacity, cnt,
-                                   m->scratch, cl, s);
-  } else {
-    e = launch_compact<P64, false>(static_cast<const P64*>(m->buckets), static_cast<P64*>(d_out), n, *pred,
-                                   TableRef<P64>{static_cast<const P64*>(m->buckets), m->sp}, capacity, cnt,
-                                   m->scratch, cl, s);
-  }
-  if (e != cudaSuccess) return cuda_status(e);
-  if ((st = after_launch()) != HX_OK) return st;
-  if (h_count) {
-    unsigned long long c = 0;
-    unsigned int err = 0;
-    HX_CUDA(cudaMemcpyAsync(&c, cnt, sizeof(c), cudaMemcpyDeviceToHost, s));
-    HX_CUDA(cudaMemcpyAsync(&err, static_cast<char*>(m->scratch) + 4, sizeof(err), cudaMemcpyDeviceToHost, s));
-    HX_CUDA(cudaStreamSynchronize(s));
-    *h_count = c;
-    if (err) return HX_ERR_TIMEOUT;
-    if (c > capacity) return HX_ERR_CAPACITY;
-  }
-  return HX_OK;
+  return extract<false>(m, pred, d_out, capacity, d_count, h_count, stream);
+}
+
+hx_status hx_extract_keys(hx_map* m, const hx_pred* pred, void* d_out_keys, uint64_t capacity, uint64_t* d_count,
+                          uint64_t* h_count, hx_stream stream) {
+  return extract<true>(m, pred, d_out_keys, capacity, d_count, h_count, stream);
 }
 
 hx_status hx_resize(hx_map* m, int new_size_power, hx_stream stream) {
@@ -941,6 +956,19 @@ hx_status hx_peek_status(hx_map* m, int32_t* out, hx_stream stream) {
   HX_CUDA(cudaMemcpyAsync(&m->info->err, &inv, sizeof(int), cudaMemcpyHostToDevice, s));
   HX_CUDA(cudaStreamSynchronize(s));
   *out = v;
+  return HX_OK;
+}
+
+hx_status hx_map_device_view(hx_map* m, hx_device_view* out) {
+  if (!valid_map(m) || !out) return HX_ERR_INVALID_ARG;
+  out->buckets = m->buckets;
+  out->size_power = m->sp;
+  out->reserved = 0;
+  out->fill = &m->info->fill;
+  out->tombstones = &m->info->tombstones;
+  out->max_probe = &m->info->max_probe;
+  out->err = &m->info->err;
+  m->fill_ub = nslots(m);  // device-side inserts are invisible to the host bound
   return HX_OK;
 }
 

@@ -17,6 +17,7 @@
 // host turns that word into HX_ERR_TIMEOUT.
 #pragma once
 #include "hx_device.cuh"
+#include <type_traits>
 
 namespace hx {
 
@@ -211,6 +212,14 @@ __device__ __forceinline__ void load_vec(const T* p, T (&v)[16 / sizeof(T)]) {
   memcpy(&v[0], &q, 16);
 }
 
+// What a selected element writes: the element itself, or (O = its key type)
+// only the key of a bucket pair (extractKeysByPattern).
+template <class T, class O>
+__device__ __forceinline__ O project(const T& x) {
+  if constexpr (std::is_same<T, O>::value) return x;
+  else return x.first;
+}
+
 // clean_tombstones mode (CLEAN): the input is the bucket array itself. Every
 // TOMBSTONE bucket and every selected (moved) bucket is rewritten to
 // (EMPTY, 0) after it has been read, the last tile takes the moved count off
@@ -223,8 +232,8 @@ struct CleanArgs {
   unsigned long long* fill;
 };
 
-template <class T, int BLOCK, int R, bool CLEAN>
-__global__ void __launch_bounds__(BLOCK) k_compact(const T* __restrict__ in, T* __restrict__ out, uint64_t n,
+template <class T, class O, int BLOCK, int R, bool CLEAN>
+__global__ void __launch_bounds__(BLOCK) k_compact(const T* __restrict__ in, O* __restrict__ out, uint64_t n,
                                                   hx_pred pr, typename ElemOps<T>::Ctx ctx, uint64_t capacity,
                                                   unsigned long long* d_count, ScanScratch sc, bool vec,
                                                   CleanArgs cl) {
@@ -235,7 +244,7 @@ __global__ void __launch_bounds__(BLOCK) k_compact(const T* __restrict__ in, T* 
   __shared__ unsigned long long s_tile, s_prefix;
   __shared__ unsigned s_total;
   extern __shared__ __align__(16) unsigned char s_raw[];
-  T* s_out = reinterpret_cast<T*>(s_raw);
+  O* s_out = reinterpret_cast<O*>(s_raw);
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if constexpr (CLEAN) {
@@ -310,7 +319,7 @@ __global__ void __launch_bounds__(BLOCK) k_compact(const T* __restrict__ in, T* 
     unsigned o = wbase + pre[r];
 #pragma unroll
     for (int q = 0; q < E; ++q)
-      if (f[r] & (1u << q)) s_out[o++] = x[r][q];
+      if (f[r] & (1u << q)) s_out[o++] = project<T, O>(x[r][q]);
   }
   __syncthreads();
   const unsigned total = s_total;
@@ -351,16 +360,16 @@ inline ScanScratch carve_scratch(void* p, uint64_t tiles) {
 
 // Launch one compaction pass (n > 0). The scratch must hold
 // scan_scratch_bytes(compact_tiles<T>(n)) bytes; it is zeroed here.
-template <class T, bool CLEAN>
-inline cudaError_t launch_compact(const T* in, T* out, uint64_t n, const hx_pred& pr,
+template <class T, bool CLEAN, class O = T>
+inline cudaError_t launch_compact(const T* in, O* out, uint64_t n, const hx_pred& pr,
                                   typename ElemOps<T>::Ctx ctx, uint64_t capacity, unsigned long long* d_count,
                                   void* scratch, CleanArgs cl, cudaStream_t s) {
   const uint64_t tiles = compact_tiles<T>(n);
   cudaError_t e = cudaMemsetAsync(scratch, 0, scan_scratch_bytes(tiles), s);
   if (e != cudaSuccess) return e;
   const bool vec = ((uintptr_t)in % 16) == 0;
-  const size_t smem = (size_t)compact_tile_elems<T>() * sizeof(T);
-  auto kern = k_compact<T, kCompactBlock, kCompactR, CLEAN>;
+  const size_t smem = (size_t)compact_tile_elems<T>() * sizeof(O);
+  auto kern = k_compact<T, O, kCompactBlock, kCompactR, CLEAN>;
   kern<<<(unsigned)tiles, kCompactBlock, smem, s>>>(in, out, n, pr, ctx, capacity, d_count,
                                                    carve_scratch(scratch, tiles), vec, cl);
   return cudaGetLastError();

@@ -196,6 +196,82 @@ __global__ void __launch_bounds__(256) k_serve(ServeArgs<P> a) {
   }
 }
 
+// ---- batched rehash of the tables a round needs to grow or clean ----------
+struct GrowTask {
+  void* old_table;
+  void* new_table;
+  unsigned long long old_n;
+  int new_sp;
+  unsigned map;
+};
+struct GrowChunk {
+  unsigned task;
+  unsigned count;
+  unsigned long long begin;
+};
+
+// (EMPTY, 0) into every bucket of the new tables; chunk 0 of a task also
+// resets the map's metadata (a rehash drops tombstones and re-counts fill).
+template <class P>
+__global__ void __launch_bounds__(256) k_grow_fill(const GrowTask* tasks, const GrowChunk* chunks, unsigned n_chunks,
+                                                   DInfo* info) {
+  for (unsigned c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+    const GrowChunk ch = chunks[c];
+    const GrowTask tk = tasks[ch.task];
+    P* t = static_cast<P*>(tk.new_table);
+    P e;
+    e.first = PairTraits<P>::EMPTY;
+    e.second = 0;
+    for (unsigned k = threadIdx.x; k < ch.count; k += blockDim.x) t[ch.begin + k] = e;
+    if (ch.begin == 0 && threadIdx.x == 0) {
+      DInfo* inf = info + tk.map;
+      inf->fill = 0;
+      inf->tombstones = 0;
+      inf->max_probe = 0;
+    }
+  }
+}
+
+// Every valid pair of the old tables into the new ones (thread per bucket).
+template <class P>
+__global__ void __launch_bounds__(256) k_grow_move(const GrowTask* tasks, const GrowChunk* chunks, unsigned n_chunks,
+                                                   DInfo* info) {
+  constexpr int BT = sizeof(P) == 8 ? 4 : 2;
+  __shared__ unsigned s_ins, s_max, s_fail;
+  const int lane = threadIdx.x & 31;
+  for (unsigned c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+    if (threadIdx.x == 0) s_ins = s_max = s_fail = 0;
+    __syncthreads();
+    const GrowChunk ch = chunks[c];
+    const GrowTask tk = tasks[ch.task];
+    const P* o = static_cast<const P*>(tk.old_table);
+    P* t = static_cast<P*>(tk.new_table);
+    unsigned ins = 0, maxd = 0;
+    bool fail = false;
+    for (unsigned k = threadIdx.x; k < ch.count; k += blockDim.x) {
+      const P pr = o[ch.begin + k];
+      if (pr.first != PairTraits<P>::EMPTY && pr.first != PairTraits<P>::TOMB)
+        insert_one_t1<P, BT>(t, tk.new_sp, pr.first, pr.second, ins, maxd, fail);
+    }
+    ins = __reduce_add_sync(0xffffffffu, ins);
+    maxd = __reduce_max_sync(0xffffffffu, maxd);
+    const bool anyfail = __any_sync(0xffffffffu, fail);
+    if (lane == 0) {
+      if (ins) atomicAdd(&s_ins, ins);
+      if (maxd) atomicMax(&s_max, maxd);
+      if (anyfail) atomicExch(&s_fail, 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      DInfo* inf = info + tk.map;
+      if (s_ins) atomicAdd(&inf->fill, (unsigned long long)s_ins);
+      if (s_max) atomicMax(&inf->max_probe, s_max);
+      if (s_fail) atomicExch(&inf->err, HX_STATUS_FAIL);
+    }
+    __syncthreads();
+  }
+}
+
 static uint64_t now_ns() {
   return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
              std::chrono::steady_clock::now().time_since_epoch())
@@ -235,6 +311,11 @@ struct Slot {
   std::vector<uint64_t> tags;
   std::vector<std::pair<unsigned, uint64_t>> inserts;  // (map, keys) launched in this round
   std::vector<std::pair<unsigned, uint64_t>> erases;   // (map, keys) launched in this round
+  GrowTask* h_tasks = nullptr;
+  GrowChunk* h_chunks = nullptr;
+  GrowTask* d_tasks = nullptr;
+  GrowChunk* d_chunks = nullptr;
+  size_t chunk_cap = 0;
 };
 
 }  // namespace hx
@@ -365,6 +446,11 @@ hx_status hx_server_create(hx_server** out, int key_bytes, uint64_t memory_budge
     if (e == cudaSuccess)
       e = cudaMalloc(reinterpret_cast<void**>(&sl.d_cnt), (2 + max_round_requests) * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDefault);
+    sl.chunk_cap = 1 << 16;
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&sl.h_tasks), max_maps * sizeof(GrowTask));
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&sl.h_chunks), sl.chunk_cap * sizeof(GrowChunk));
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&sl.d_tasks), max_maps * sizeof(GrowTask));
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&sl.d_chunks), sl.chunk_cap * sizeof(GrowChunk));
   }
   if (e != cudaSuccess) {
     *out = sv;
@@ -390,6 +476,10 @@ hx_status hx_server_destroy(hx_server* sv) {
     cudaFree(sl.d_reqs);
     cudaFree(sl.d_tiles);
     cudaFree(sl.d_cnt);
+    cudaFreeHost(sl.h_tasks);
+    cudaFreeHost(sl.h_chunks);
+    cudaFree(sl.d_tasks);
+    cudaFree(sl.d_chunks);
     if (sl.done) cudaEventDestroy(sl.done);
   }
   cudaFree(sv->d_maps);
@@ -483,6 +573,9 @@ static hx_status server_step(hx_server* sv, uint32_t* launched) {
   // if the live keys need it. Bounds are upper bounds, so a map never fills.
   std::vector<uint64_t> add(sv->maps.size(), 0), era(sv->maps.size(), 0);
   std::vector<char> admitted(round.size(), 1);
+  std::vector<int> grow_of(sv->maps.size(), -1);
+  std::vector<GrowTask> tasks;
+  std::vector<void*> old_tables;
   const uint64_t this_round = sv->rounds;
   for (size_t i = 0; i < round.size(); ++i) {
     const hx_request& r = round[i].r;
@@ -504,20 +597,67 @@ static hx_status server_step(hx_server* sv, uint32_t* launched) {
         admitted[i] = 0;  // cannot make room within the budget: reject this insert
         continue;
       }
-      hx_map v;
-      view_of(sv, r.map, &v);
-      st = map_rehash_view(&v, nsp, sv->s);  // on-device rehash, stream-ordered after earlier rounds
-      if (st != HX_OK) return st;
+      // one batched rehash per map and round: a second need in the same round
+      // replaces the pending target with the larger table
+      int& slot_of = grow_of[r.map];
+      void* nt = nullptr;
+      HX_CUDA(cudaMallocAsync(&nt, nbytes, sv->s));
+      if (slot_of < 0) {
+        slot_of = (int)tasks.size();
+        tasks.push_back(GrowTask{m.table, nt, 1ull << m.sp, nsp, r.map});
+        old_tables.push_back(m.table);
+      } else {
+        HX_CUDA(cudaFreeAsync(tasks[slot_of].new_table, sv->s));  // never used
+        tasks[slot_of].new_table = nt;
+        tasks[slot_of].new_sp = nsp;
+      }
       sv->used = sv->used - m.bytes + nbytes;
       sv->st.growths++;
       sv->st.growth_bytes += nbytes;
-      m.table = v.buckets;
+      m.table = nt;
       m.sp = nsp;
       m.bytes = nbytes;
       m.tomb_ub = 0;
       m.rehash_round = this_round;
     }
     add[r.map] += r.n;
+  }
+  if (!tasks.empty()) {
+    // chunk the old tables (move) and the new ones (fill) into pieces of 64K buckets
+    constexpr uint64_t kChunk = 1 << 16;
+    std::vector<GrowChunk> fillc, movec;
+    for (unsigned i = 0; i < tasks.size(); ++i) {
+      const uint64_t nn = 1ull << tasks[i].new_sp;
+      for (uint64_t a0 = 0; a0 < nn; a0 += kChunk) fillc.push_back(GrowChunk{i, (unsigned)std::min<uint64_t>(kChunk, nn - a0), a0});
+      for (uint64_t a0 = 0; a0 < tasks[i].old_n; a0 += kChunk)
+        movec.push_back(GrowChunk{i, (unsigned)std::min<uint64_t>(kChunk, tasks[i].old_n - a0), a0});
+    }
+    if (fillc.size() + movec.size() > sl->chunk_cap) {
+      cudaStreamSynchronize(sv->s);  // rare: grow the staging buffers
+      cudaFreeHost(sl->h_chunks);
+      cudaFree(sl->d_chunks);
+      sl->chunk_cap = (fillc.size() + movec.size()) * 2;
+      HX_CUDA(cudaMallocHost(reinterpret_cast<void**>(&sl->h_chunks), sl->chunk_cap * sizeof(GrowChunk)));
+      HX_CUDA(cudaMalloc(reinterpret_cast<void**>(&sl->d_chunks), sl->chunk_cap * sizeof(GrowChunk)));
+    }
+    std::copy(tasks.begin(), tasks.end(), sl->h_tasks);
+    std::copy(fillc.begin(), fillc.end(), sl->h_chunks);
+    std::copy(movec.begin(), movec.end(), sl->h_chunks + fillc.size());
+    cudaStream_t gs = sv->s;
+    HX_CUDA(cudaMemcpyAsync(sl->d_tasks, sl->h_tasks, tasks.size() * sizeof(GrowTask), cudaMemcpyHostToDevice, gs));
+    HX_CUDA(cudaMemcpyAsync(sl->d_chunks, sl->h_chunks, (fillc.size() + movec.size()) * sizeof(GrowChunk),
+                            cudaMemcpyHostToDevice, gs));
+    const unsigned g = (unsigned)std::min<size_t>((size_t)sm_count() * 8, std::max(fillc.size(), movec.size()));
+    if (sv->kb == 4) {
+      k_grow_fill<P32><<<g, 256, 0, gs>>>(sl->d_tasks, sl->d_chunks, (unsigned)fillc.size(), sv->d_info);
+      k_grow_move<P32><<<g, 256, 0, gs>>>(sl->d_tasks, sl->d_chunks + fillc.size(), (unsigned)movec.size(), sv->d_info);
+    } else {
+      k_grow_fill<P64><<<g, 256, 0, gs>>>(sl->d_tasks, sl->d_chunks, (unsigned)fillc.size(), sv->d_info);
+      k_grow_move<P64><<<g, 256, 0, gs>>>(sl->d_tasks, sl->d_chunks + fillc.size(), (unsigned)movec.size(), sv->d_info);
+    }
+    st = after_launch();
+    if (st != HX_OK) return st;
+    for (void* p : old_tables) HX_CUDA(cudaFreeAsync(p, gs));
   }
   // Stages per map, in admission order: a write (insert, erase) is a stage of
   // its own; consecutive queries share one stage. Every stage waits for the

@@ -155,6 +155,14 @@ hx_status hx_clean_tombstones(hx_map* map, hx_stream stream);
 hx_status hx_extract_pattern(hx_map* map, const hx_pred* pred, void* d_out, uint64_t capacity, uint64_t* d_count,
                              uint64_t* h_count, hx_stream stream);
 
+/* extractKeysByPattern(keys, rule, s) / extractAllKeys(keys, s)
+ * (hashinator.h:1199-1239): the same selection as hx_extract_pattern, writing
+ * only the key of each selected bucket (key_bytes each) in bucket order.
+ * extractAllKeys is the predicate {HX_PRED_VALID}. Counts and capacity as
+ * for hx_extract_pattern. */
+hx_status hx_extract_keys(hx_map* map, const hx_pred* pred, void* d_out_keys, uint64_t capacity, uint64_t* d_count,
+                          uint64_t* h_count, hx_stream stream);
+
 /* resize(newSizePower, targets::device, stream) = device_rehash
  * (hashinator.h:285-336, :552-566): every valid pair moves into a new table
  * of 2^new_size_power buckets in one streaming pass; tombstones are dropped.
@@ -176,6 +184,23 @@ hx_status hx_peek_status(hx_map* map, int32_t* out, hx_stream stream);
 
 /* expose_bucketdata() (hashinator.h:477-483): the device bucket array. */
 hx_status hx_bucket_data(hx_map* map, void** d_buckets, uint64_t* bucket_count);
+
+/* Device view of a map for element access from user kernels
+ * (include/hx_device_api.cuh): Hashmap::upload() / get_device_pointer()
+ * (hashinator.h:1420-1470) and the device API they enable. The pointers stay
+ * valid until the next call that reallocates the table (insert with growth,
+ * resize, destroy). Because device-side inserts bypass the host, the map's
+ * host-side fill bound becomes the table size until hx_get_info refreshes it. */
+typedef struct hx_device_view {
+  void* buckets;
+  int32_t size_power;
+  int32_t reserved;
+  unsigned long long* fill;
+  unsigned long long* tombstones;
+  unsigned int* max_probe;
+  int32_t* err;
+} hx_device_view;
+hx_status hx_map_device_view(hx_map* map, hx_device_view* out);
 
 /* Probe tuning (no reference counterpart: the reference fixes one 32-lane
  * warp per key, hashinator/defaults.h:26-38). group_width in

@@ -327,6 +327,39 @@ def test_extract_pattern(hx, oracle_mod, w):
     assert m.extract_pattern(hx.Pred.valid_key(), small, capacity=10) == om.info()["fill"]
 
 
+@pytest.mark.parametrize("w", [4, 8])
+def test_extract_keys(hx, oracle_mod, w):
+    """extractKeysByPattern / extractAllKeys: the keys of the pairs that
+    extractPattern selects, in the same bucket order."""
+    dt = _dt(w)
+    keys, vals, _, e = workloads.map_workload(30000, w, 123)
+    m = hx.Hashmap(16, w)
+    m.insert(to_dev(keys), to_dev(vals), 0.0)
+    m.erase(to_dev(e))
+    om = oracle_mod.OracleMap(16, w)
+    om.insert(keys, vals, 0.0)
+    om.erase(e)
+    b = bucket_array(m, w)
+    for hp, op in [(hx.Pred.value_even(), oracle_mod.pred(6, 2, 1, 0, 1)), (hx.Pred.valid_key(), oracle_mod.pred(8)),
+                   (hx.Pred.not_home(), oracle_mod.pred(9))]:
+        out = to_dev(np.full(1 << 16, 7, dt))
+        c = m.extract_keys_by_pattern(hp, out)
+        got = from_dev(out, dt)
+        want = _filter_buckets(oracle_mod, b, w, op)[:, 0]
+        assert c == len(want)
+        np.testing.assert_array_equal(got[:c], want)
+        assert (got[c:] == 7).all()  # nothing written past the count
+    out = to_dev(np.zeros(1 << 16, dt))
+    c = m.extract_all_keys(out)
+    ok, _ = om.mapping()
+    assert c == len(ok)
+    np.testing.assert_array_equal(np.sort(from_dev(out, dt)[:c]), ok)
+    # capacity below the count: exact count, only `capacity` keys written
+    small = to_dev(np.full(11, 7, dt))
+    assert m.extract_all_keys(small, capacity=10) == len(ok)
+    assert from_dev(small, dt)[10] == 7
+
+
 def _filter_buckets(oracle_mod, b, w, op):
     """Order-preserving CPU filter of an arbitrary bucket array (the device's)."""
     flat = np.ascontiguousarray(b.reshape(-1))
