@@ -175,7 +175,12 @@ def run_batched(args, stream, dev):
         outs.append(o)
     bf, bp = batches
     pf, pp = plans
-    tune = autotune_batch(pf, lambda: bf.clear(stream=stream), stream=stream)
+    if args.batched_tuning:
+        g, b_, t_ = args.batched_tuning
+        pf.set_tuning(g, b_, t_, stream=stream)
+        tune = {"best": (g, b_, t_)}
+    else:
+        tune = autotune_batch(pf, lambda: bf.clear(stream=stream), stream=stream)
 
     def timed(fn, reps):
         ts = []
@@ -252,7 +257,8 @@ def run_serving(args, dev):
         used, _ = srv.memory()
         sst = srv.stats()
         results.append({"rounds": sst["rounds"], "growths": sst["growths"], "max_stage_depth": sst["max_stage_depth"],
-                        "host_ms_forming_rounds": round(sst["host_ns_step"] / 1e6, 1),"offered_req_s": rate, "offered_Mkeys_s": round(total_keys / (arrival.max() / 1e9) / 1e6, 1),
+                        "host_ms_forming_rounds": round(sst["host_ns_step"] / 1e6, 1), "offered_req_s": rate,
+                        "offered_Mkeys_s": round(total_keys / (arrival.max() / 1e9) / 1e6, 1),
                         "p50_us": round(float(np.percentile(lat, 50)), 1),
                         "p99_us": round(float(np.percentile(lat, 99)), 1),
                         "sustained_Mkeys_s": round(total_keys / span / 1e6, 1),
@@ -361,7 +367,7 @@ def run_streaming(args, stream, dev, peak):
     import torch
     import hashinator_gb300 as hx
     from hashinator_gb300 import workloads
-    n = 1 << 28
+    n = 1 << args.stream_log_n
     x = torch.randint(0, 2**31 - 1, (n,), dtype=torch.int64, device=dev, generator=torch.Generator(device=dev).manual_seed(7))
     x = (x * 2 + (x >> 17 & 1)).to(torch.int32)  # uniform over the 32-bit range, as int32 bits
     out = torch.empty_like(x)
@@ -396,6 +402,13 @@ def run_streaming(args, stream, dev, peak):
     res["extract_pattern_value_even"] = {"selected": int(c), "expected": int((vals % 2 == 0).sum()),
                                          "ms": round(t * 1e3, 3), "GB_s": round(byts / t / 1e9, 1),
                                          "frac": round(byts / t / 1e9 / peak, 4)}
+    ek = torch.empty(1 << 26, dtype=torch.int32, device=dev)
+    ck = m.extract_all_keys(ek, stream=stream)
+    t = _ev_time(stream, lambda: m.extract_keys_by_pattern(hx.Pred.valid_key(), ek, capacity=1 << 26,
+                                                           stream=stream, d_count=dc))
+    byts = 8 * (1 << 27) + 4 * ck
+    res["extract_all_keys"] = {"selected": int(ck), "expected": 1 << 26, "ms": round(t * 1e3, 3),
+                               "GB_s": round(byts / t / 1e9, 1), "frac": round(byts / t / 1e9 / peak, 4)}
     m.close()
     return res
 
@@ -625,7 +638,8 @@ def run_ours(args):
         serving = run_serving(args, dev)
     lf_sweep = streaming = None
     if not args.no_extra:
-        lf_sweep = run_lf_sweep(args, stream, dev, peak)
+        if not args.no_lf_sweep:
+            lf_sweep = run_lf_sweep(args, stream, dev, peak)
         streaming = run_streaming(args, stream, dev, peak)
 
     if rank == 0:
@@ -661,8 +675,12 @@ def main():
     ap.add_argument("--e2e-chunks", type=int, default=8)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-maps", type=int, default=4096)
+    ap.add_argument("--batched-tuning", type=int, nargs=3, metavar=("GROUP", "BLOCK", "TILE"),
+                    help="fixed lanes-per-key, block size and tile keys instead of the autotuner")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the LF sweep and the streaming primitives")
+    ap.add_argument("--no-lf-sweep", action="store_true", help="skip the LF sweep only")
+    ap.add_argument("--stream-log-n", type=int, default=28, help="log2 of the streaming-primitive element count")
     ap.add_argument("--serving-maps", type=int, default=1024)
     ap.add_argument("--serving-requests", type=int, default=20000)
     ap.add_argument("--serving-rates", type=float, nargs="+", default=[2.5e5, 5e5, 1e6, 2e6, 4e6])

@@ -116,6 +116,9 @@ _SIGS = {
                         ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.c_void_p],
     "hx_map_device_view": [ctypes.c_void_p, ctypes.c_void_p],
     "hx_resize": [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p],
+    "hx_insert_index": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_float, ctypes.c_void_p],
+    "hx_resize_to_lf": [ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p],
+    "hx_perform_cleanup_tasks": [ctypes.c_void_p, ctypes.c_void_p],
     "hx_clear": [ctypes.c_void_p, ctypes.c_void_p],
     "hx_get_info": [ctypes.c_void_p, ctypes.POINTER(Info), ctypes.c_void_p],
     "hx_peek_status": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p],
@@ -371,6 +374,17 @@ class Hashmap:
         _check(self._h.hx_resize(self._m, new_size_power, _stream(stream)), "hx_resize")
 
     device_rehash = resize
+
+    def resize_to_lf(self, target_lf: float = 0.5, stream=None) -> None:
+        _check(self._h.hx_resize_to_lf(self._m, target_lf, _stream(stream)), "hx_resize_to_lf")
+
+    def perform_cleanup_tasks(self, stream=None) -> None:
+        _check(self._h.hx_perform_cleanup_tasks(self._m, _stream(stream)), "hx_perform_cleanup_tasks")
+
+    def insert_index(self, keys, target_lf: float = 0.5, stream=None, n: int | None = None) -> None:
+        """insertIndex(keys, len, targetLF): keys[i] gets the value i."""
+        n = _numel(keys) if n is None else n
+        _check(self._h.hx_insert_index(self._m, _ptr(keys), n, target_lf, _stream(stream)), "hx_insert_index")
 
     def clear(self, stream=None) -> None:
         _check(self._h.hx_clear(self._m, _stream(stream)), "hx_clear")

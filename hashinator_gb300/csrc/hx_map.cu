@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(256) k_insert(const typename PairTraits<P>::K*
         val = pr.second;
       } else {
         key = keys[i];
-        val = vals[i];
+        val = vals ? vals[i] : (V)i;  // no values: insertIndex
       }
       if (key != PairTraits<P>::EMPTY && key != PairTraits<P>::TOMB) {
         unsigned d1 = 0;
@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(256) k_insert_t1(const typename PairTraits<P>:
           val[u] = pr.second;
         } else {
           key[u] = keys[i];
-          val[u] = vals[i];
+          val[u] = vals ? vals[i] : (V)i;  // no values: insertIndex
         }
         act[u] = key[u] != EMPTY && key[u] != PairTraits<P>::TOMB;
       }
@@ -830,6 +830,20 @@ hx_status hx_insert(hx_map* m, const void* d_keys, const void* d_vals, uint64_t 
                    : launch_insert<P64>(m, d_keys, d_vals, nullptr, n, nullptr, s);
 }
 
+hx_status hx_insert_index(hx_map* m, const void* d_keys, uint64_t n, float target_lf, hx_stream stream) {
+  if (!valid_map(m)) return HX_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  HX_CUDA(cudaMemsetAsync(&m->info->err, 0, sizeof(int), s));
+  if (n == 0) return HX_OK;
+  if (!d_keys) return HX_ERR_INVALID_ARG;
+  hx_status st = maybe_grow(m, n, target_lf, s);
+  if (st != HX_OK) return st;
+  HX_CUDA(cudaMemsetAsync(&m->info->err, 0, sizeof(int), s));
+  m->fill_ub += n;
+  return is_p32(m) ? launch_insert<P32>(m, d_keys, nullptr, nullptr, n, nullptr, s)
+                   : launch_insert<P64>(m, d_keys, nullptr, nullptr, n, nullptr, s);
+}
+
 hx_status hx_insert_pairs(hx_map* m, const void* d_pairs, uint64_t n, float target_lf, hx_stream stream) {
   if (!valid_map(m)) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -929,6 +943,37 @@ hx_status hx_clear(hx_map* m, hx_stream stream) {
   k_info_reset<<<1, 1, 0, s>>>(m->info);
   m->fill_ub = 0;
   return after_launch();
+}
+
+hx_status hx_resize_to_lf(hx_map* m, float target_lf, hx_stream stream) {
+  if (!valid_map(m) || !(target_lf > 0.0f)) return HX_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  DInfo di;
+  hx_status st = read_info(m, &di, s);
+  if (st != HX_OK) return st;
+  int sp = m->sp;
+  while ((float)di.fill / (float)(1ull << sp) > target_lf) {  // load_factor() > targetLF
+    if (++sp > 31) return HX_ERR_OOM;
+  }
+  return sp == m->sp ? HX_OK : rehash(m, sp, s);
+}
+
+hx_status hx_perform_cleanup_tasks(hx_map* m, hx_stream stream) {
+  if (!valid_map(m)) return HX_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  DInfo di;
+  hx_status st = read_info(m, &di, s);
+  if (st != HX_OK) return st;
+  if (di.tombstones && (float)di.tombstones / (float)nslots(m) > 0.025f) {  // tombstone_ratio() > 0.025
+    if ((st = hx_clean_tombstones(m, stream)) != HX_OK) return st;
+    if ((st = read_info(m, &di, s)) != HX_OK) return st;
+  }
+  // currentMaxBucketOverflow > BUCKET_OVERFLOW: grow until the probe bound fits one 32-bucket window
+  while (di.max_probe > 32 && m->sp < 31) {
+    if ((st = rehash(m, m->sp + 1, s)) != HX_OK) return st;
+    if ((st = read_info(m, &di, s)) != HX_OK) return st;
+  }
+  return HX_OK;
 }
 
 hx_status hx_get_info(hx_map* m, hx_info* out, hx_stream stream) {

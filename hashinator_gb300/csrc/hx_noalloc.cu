@@ -20,12 +20,13 @@
 namespace hx {
 
 constexpr uint64_t kNoAllocTileElems = (uint64_t)kScanBlock * kScanR * 4;
-constexpr uint64_t kNoAllocTiles = HX_NOALLOC_SCAN_MAX_N / kNoAllocTileElems;
-static_assert(HX_NOALLOC_SCAN_MAX_N % kNoAllocTileElems == 0, "whole tiles");
-static_assert(HX_NOALLOC_SCAN_SCRATCH_BYTES == 256 + 8 * kNoAllocTiles, "ticket/error words + tile statuses");
+constexpr uint64_t kNoAllocTiles = (HX_NOALLOC_SCAN_MAX_N + kNoAllocTileElems - 1) / kNoAllocTileElems;
+static_assert(256 + 8 * kNoAllocTiles <= HX_NOALLOC_SCAN_SCRATCH_BYTES, "ticket/error words + tile statuses fit");
 
 // Look-back scratch of the no-allocation scan: 256 B of ticket and error
-// words, then one 8-byte status word per tile (524,544 B in all).
+// words, then one 8-byte status word per tile. The array keeps the size the
+// header promises (524,544 B, room for tiles as small as 4096 elements); the
+// scan's tiles of 12,288 elements use at most 175,024 B of it.
 static __device__ __align__(256) unsigned char g_noalloc_scan_scratch[HX_NOALLOC_SCAN_SCRATCH_BYTES];
 
 // Device address of the array, looked up once per device with that device

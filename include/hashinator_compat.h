@@ -9,6 +9,8 @@
  *   split::SplitVector<T>         splitvector/splitvec.h:83 (managed memory, minimal surface)
  *   split::tools::copy_if         splitvector/split_tools.h:1129-1223
  *   split::tools::split_prefix_scan  split_tools.h:363-418
+ *   device API (upload/download, device_find/insert/erase, iterators,
+ *   warpInsert/warpFind/warpErase)   hashinator.h:853-1126, 1417-1769
  *
  * Behaviour matches the reference's: every accelerated call blocks the host
  * until its stream is done (hashinator/hashers.h:55 and siblings), CUDA
@@ -28,6 +30,7 @@
 #include <type_traits>
 
 #include "hx.h"
+#include "hx_device_api.cuh"
 
 namespace hxcompat {
 inline void check(hx_status st, const char* what) {
@@ -174,9 +177,22 @@ __global__ void count_tiles(const T* in, size_t n, Rule rule, uint32_t* counts) 
   if (threadIdx.x == 0) counts[blockIdx.x] = s;
 }
 
-template <typename T, typename Rule>
-__global__ void scatter_tiles(const T* in, size_t n, Rule rule, const uint32_t* offsets, T* out, size_t cap,
-                              unsigned long long* total, size_t nblocks) {
+struct Identity {
+  template <typename T>
+  __device__ const T& operator()(const T& x) const {
+    return x;
+  }
+};
+struct KeyOf {
+  template <typename T>
+  __device__ auto operator()(const T& x) const -> decltype(x.first) {
+    return x.first;
+  }
+};
+
+template <typename T, typename O, typename Rule, typename Proj>
+__global__ void scatter_tiles(const T* in, size_t n, Rule rule, const uint32_t* offsets, O* out, size_t cap,
+                              unsigned long long* total, size_t nblocks, Proj proj) {
   __shared__ uint32_t warp_base[32];
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -201,14 +217,15 @@ __global__ void scatter_tiles(const T* in, size_t n, Rule rule, const uint32_t* 
   __syncthreads();
   if (sel) {
     const size_t dst = (size_t)offsets[blockIdx.x] + warp_base[warp] + __popc(b & ((1u << lane) - 1u));
-    if (dst < cap) out[dst] = x;
+    if (dst < cap) out[dst] = proj(x);
   }
 }
 
 // Stable compaction with a user functor: per-block counts, libhx exclusive
-// scan of the counts, order-preserving scatter.
-template <typename T, typename Rule>
-size_t copy_if_functor(const T* in, T* out, size_t n, size_t cap, Rule rule, cudaStream_t s) {
+// scan of the counts, order-preserving scatter of proj(x) (the element, or
+// the key of a bucket pair).
+template <typename T, typename O, typename Rule, typename Proj>
+size_t copy_if_functor(const T* in, O* out, size_t n, size_t cap, Rule rule, Proj proj, cudaStream_t s) {
   if (n == 0) return 0;
   const unsigned block = 256;
   const size_t nb = (n + block - 1) / block;
@@ -219,7 +236,7 @@ size_t copy_if_functor(const T* in, T* out, size_t n, size_t cap, Rule rule, cud
   total = reinterpret_cast<unsigned long long*>(counts + 2 * nb);  // 8-byte aligned: 2*nb words
   count_tiles<<<(unsigned)nb, block, 0, s>>>(in, n, rule, counts);
   hxcompat::check(hx_exclusive_scan_u32(counts, offsets, nb, nullptr, 0, s), "hx_exclusive_scan_u32");
-  scatter_tiles<<<(unsigned)nb, block, 0, s>>>(in, n, rule, offsets, out, cap, total, nb);
+  scatter_tiles<<<(unsigned)nb, block, 0, s>>>(in, n, rule, offsets, out, cap, total, nb, proj);
   unsigned long long h = 0;
   hxcompat::check_cuda(cudaMemcpyAsync(&h, total, sizeof(h), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
   hxcompat::check_cuda(cudaFreeAsync(counts, s), "cudaFreeAsync");
@@ -246,7 +263,8 @@ void copy_if(SplitVector<T>& input, SplitVector<T>& output, Rule rule, cudaStrea
     if (st != HX_OK && st != HX_ERR_CAPACITY) hxcompat::check(st, "hx_copy_if");
     c = (size_t)h;
   } else {
-    c = detail::copy_if_functor(input.data(), output.data(), input.size(), output.size(), rule, s);
+    c = detail::copy_if_functor(input.data(), output.data(), input.size(), output.size(), rule, detail::Identity{},
+                                s);
   }
   output.erase(output.data() + (c < output.size() ? c : output.size()), output.end());
 }
@@ -255,7 +273,7 @@ void copy_if(SplitVector<T>& input, SplitVector<T>& output, Rule rule, cudaStrea
  * (split_tools.h:1211): returns the count. */
 template <typename T, typename Rule>
 size_t copy_if(T* input, T* output, size_t size, Rule rule, void* /*stack*/, size_t /*max_size*/, cudaStream_t s = 0) {
-  return detail::copy_if_functor(input, output, size, size, rule, s);
+  return detail::copy_if_functor(input, output, size, size, rule, detail::Identity{}, s);
 }
 
 /* split_prefix_scan(in, out, stream) (split_tools.h:363): exclusive sum of
@@ -281,7 +299,15 @@ class Hashmap {
   static_assert(EMPTYBUCKET == std::numeric_limits<KEY_TYPE>::max() && TOMBSTONE == EMPTYBUCKET - 1,
                 "libhx uses the reference's default sentinels");
   using pair_t = hash_pair<KEY_TYPE, VAL_TYPE>;
+  using view_t = hx_device::MapView<KEY_TYPE, VAL_TYPE>;
   hx_map* m_ = nullptr;
+  hx_device_view dv_{};      // what the device copy works on (refreshed by upload())
+  Hashmap* d_self_ = nullptr;  // the device copy that upload() returns
+
+  __host__ __device__ view_t view() const { return view_t::from(dv_); }
+  __device__ pair_t* dbuckets() const { return static_cast<pair_t*>(dv_.buckets); }
+  __device__ size_t dsize() const { return (size_t)1 << dv_.size_power; }
+  __device__ static bool valid(KEY_TYPE k) { return k != EMPTYBUCKET && k != TOMBSTONE; }
 
   void sync(cudaStream_t s) const { hxcompat::check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize"); }
   hx_info info(cudaStream_t s = 0) const {
@@ -299,6 +325,7 @@ class Hashmap {
   Hashmap(const Hashmap&) = delete;
   Hashmap& operator=(const Hashmap&) = delete;
   ~Hashmap() {
+    if (d_self_) cudaFree(d_self_);
     if (m_) hx_map_destroy(m_);
   }
 
@@ -345,6 +372,60 @@ class Hashmap {
     sync(s);
   }
 
+  /* insertIndex(keys, len, targetLF, s) (hashinator.h:1339): keys[i] -> i. */
+  template <bool prefetches = true>
+  void insertIndex(KEY_TYPE* keys, size_t len, float targetLF = 0.5, cudaStream_t s = 0) {
+    hxcompat::check(hx_insert_index(m_, keys, len, targetLF, s), "hx_insert_index");
+    sync(s);
+  }
+  /* resize_to_lf(targetLF, targets, s) (hashinator.h:530). */
+  void resize_to_lf(float targetLF = 0.5, targets = targets::device, cudaStream_t s = 0) {
+    hxcompat::check(hx_resize_to_lf(m_, targetLF, s), "hx_resize_to_lf");
+  }
+  /* performCleanupTasks(s) (hashinator.h:643). */
+  template <bool prefetches = true>
+  void performCleanupTasks(cudaStream_t s = 0) {
+    hxcompat::check(hx_perform_cleanup_tasks(m_, s), "hx_perform_cleanup_tasks");
+  }
+
+  /* extractKeysByPattern(SplitVector<KEY>&, Rule, s) (hashinator.h:1199):
+   * the keys of the buckets where the rule holds, in bucket order. */
+  template <bool prefetches = true, typename Rule>
+  size_t extractKeysByPattern(split::SplitVector<KEY_TYPE>& elements, Rule rule, cudaStream_t s = 0) {
+    void* b = nullptr;
+    uint64_t nb = 0;
+    hxcompat::check(hx_bucket_data(m_, &b, &nb), "hx_bucket_data");
+    elements.resize(nb);
+    size_t c;
+    if constexpr (std::is_same<Rule, hx_pred>::value) {
+      uint64_t h = 0;
+      const hx_status st = hx_extract_keys(m_, &rule, elements.data(), nb, nullptr, &h, s);
+      if (st != HX_OK && st != HX_ERR_CAPACITY) hxcompat::check(st, "hx_extract_keys");
+      c = (size_t)h;
+    } else {
+      c = split::tools::detail::copy_if_functor(static_cast<pair_t*>(b), elements.data(), nb, nb, rule,
+                                                split::tools::detail::KeyOf{}, s);
+    }
+    elements.erase(elements.data() + c, elements.end());
+    return c;
+  }
+  template <bool prefetches = true, typename Rule>
+  size_t extractKeysByPattern(split::SplitVector<KEY_TYPE>& elements, Rule rule, void* /*stack*/,
+                              size_t /*max_size*/, cudaStream_t s = 0) {
+    return extractKeysByPattern<prefetches>(elements, rule, s);
+  }
+  /* extractAllKeys(SplitVector<KEY>&, s) (hashinator.h:1224). */
+  template <bool prefetches = true>
+  size_t extractAllKeys(split::SplitVector<KEY_TYPE>& elements, cudaStream_t s = 0) {
+    hx_pred p{HX_PRED_VALID, HX_FIELD_KEY, 0, 0, 0, 0};
+    return extractKeysByPattern<prefetches>(elements, p, s);
+  }
+  template <bool prefetches = true>
+  size_t extractAllKeys(split::SplitVector<KEY_TYPE>& elements, void* /*stack*/, size_t /*max_size*/,
+                        cudaStream_t s = 0) {
+    return extractAllKeys<prefetches>(elements, s);
+  }
+
   /* extractPattern(hash_pair*, Rule, stream) (hashinator.h:1168): bucket
    * order; the output must hold the result. */
   template <typename Rule>
@@ -358,7 +439,8 @@ class Hashmap {
       if (st != HX_OK && st != HX_ERR_CAPACITY) hxcompat::check(st, "hx_extract_pattern");
       return (size_t)c;
     } else {
-      return split::tools::detail::copy_if_functor(static_cast<pair_t*>(b), elements, nb, nb, rule, s);
+      return split::tools::detail::copy_if_functor(static_cast<pair_t*>(b), elements, nb, nb, rule,
+                                                   split::tools::detail::Identity{}, s);
     }
   }
   /* extractPattern(SplitVector&, Rule, stream) (hashinator.h:1155): resized
@@ -404,6 +486,130 @@ class Hashmap {
   void optimizeGPU(cudaStream_t = 0) {}
   void optimizeCPU(cudaStream_t = 0) {}
   hx_map* handle() { return m_; }
+
+  // ---- device API (hashinator.h:853-1126, 1417-1769) ----
+  /* upload(s) (hashinator.h:1417): a device copy of this map for kernels;
+   * call it again after any host call that may reallocate the table. */
+  template <bool prefetches = true>
+  Hashmap* upload(cudaStream_t s = 0) {
+    hxcompat::check(hx_map_device_view(m_, &dv_), "hx_map_device_view");
+    if (!d_self_) hxcompat::check_cuda(cudaMalloc(&d_self_, sizeof(Hashmap)), "cudaMalloc");
+    hxcompat::check_cuda(cudaMemcpyAsync(d_self_, this, sizeof(Hashmap), cudaMemcpyHostToDevice, s),
+                         "cudaMemcpyAsync");
+    sync(s);
+    return d_self_;
+  }
+  Hashmap* get_device_pointer() { return d_self_; }
+  /* download(s) (hashinator.h:1458): after device-side work, grow if the probe
+   * bound passed one 32-bucket window, else drop tombstones. */
+  void download(cudaStream_t s = 0) {
+    const hx_info i = info(s);
+    if (i.current_max_bucket_overflow > 32) {
+      device_rehash(i.size_power + 1, s);
+    } else if (i.tombstone_counter > 0) {
+      clean_tombstones(s);
+    }
+  }
+
+  /* device_iterator (hashinator.h:1470): walks the valid buckets. */
+  template <bool CONST>
+  class iterator_t {
+    using map_t = typename std::conditional<CONST, const Hashmap, Hashmap>::type;
+    using ref_t = typename std::conditional<CONST, const pair_t&, pair_t&>::type;
+    using ptr_t = typename std::conditional<CONST, const pair_t*, pair_t*>::type;
+    size_t index = 0;
+    map_t* table = nullptr;
+
+   public:
+    __device__ iterator_t() {}
+    __device__ iterator_t(map_t& t, size_t i) : index(i), table(&t) {}
+    __device__ size_t getIndex() { return index; }
+    __device__ iterator_t& operator++() {
+      ++index;
+      while (index < table->dsize() && !valid(table->dbuckets()[index].first)) ++index;
+      return *this;
+    }
+    __device__ iterator_t operator++(int) {
+      iterator_t t = *this;
+      ++(*this);
+      return t;
+    }
+    __device__ bool operator==(iterator_t o) const { return table == o.table && index == o.index; }
+    __device__ bool operator!=(iterator_t o) const { return !(*this == o); }
+    __device__ ref_t operator*() const { return table->dbuckets()[index]; }
+    __device__ ptr_t operator->() const { return &table->dbuckets()[index]; }
+  };
+  using device_iterator = iterator_t<false>;
+  using const_device_iterator = iterator_t<true>;
+
+  __device__ device_iterator device_end() { return device_iterator(*this, dsize()); }
+  __device__ const_device_iterator device_end() const { return const_device_iterator(*this, dsize()); }
+  __device__ device_iterator device_begin() {
+    size_t i = 0;
+    while (i < dsize() && !valid(dbuckets()[i].first)) ++i;
+    return device_iterator(*this, i);
+  }
+  __device__ const_device_iterator device_begin() const {
+    size_t i = 0;
+    while (i < dsize() && !valid(dbuckets()[i].first)) ++i;
+    return const_device_iterator(*this, i);
+  }
+  __device__ device_iterator device_find(KEY_TYPE key) {
+    const int64_t i = view().device_find(key);
+    return i < 0 ? device_end() : device_iterator(*this, (size_t)i);
+  }
+  __device__ const_device_iterator device_find(KEY_TYPE key) const {
+    const int64_t i = view().device_find(key);
+    return i < 0 ? device_end() : const_device_iterator(*this, (size_t)i);
+  }
+  __device__ size_t device_count(const KEY_TYPE& key) const { return view().device_count(key); }
+  __device__ size_t device_erase(const KEY_TYPE& key) { return view().device_erase(key); }
+  /* device_erase(iterator) (hashinator.h:1673): tombstone the bucket, return
+   * the next valid one. */
+  __device__ device_iterator device_erase(device_iterator pos) {
+    pair_t* b = &dbuckets()[pos.getIndex()];
+    const KEY_TYPE item = b->first;
+    if (valid(item) && view().cas_key(reinterpret_cast<typename view_t::Bucket*>(b), item, TOMBSTONE)) {
+      atomicAdd(dv_.fill, 0ull - 1ull);
+      atomicAdd(dv_.tombstones, 1ull);
+    }
+    return ++pos;
+  }
+  template <bool skipOverWrites = false>
+  __device__ bool set_element(const KEY_TYPE& key, VAL_TYPE val) {
+    return view().template set_element<skipOverWrites>(key, val);
+  }
+  template <bool skipOverWrites = false>
+  __device__ hash_pair<device_iterator, bool> device_insert(hash_pair<KEY_TYPE, VAL_TYPE> e) {
+    const bool n = set_element<skipOverWrites>(e.first, e.second);
+    return hash_pair<device_iterator, bool>(device_find(e.first), n);
+  }
+  /* read_element (hashinator.h:1750): the reference asserts on a missing key;
+   * here the map's status becomes fail and a zero is returned. */
+  __device__ const VAL_TYPE& read_element(const KEY_TYPE& key) const {
+    const int64_t i = view().device_find(key);
+    if (i >= 0) return dbuckets()[i].second;
+    atomicExch(dv_.err, HX_STATUS_FAIL);
+    return missing_value();
+  }
+  template <bool skipOverWrites = false>
+  __device__ void warpInsert(const KEY_TYPE& key, const VAL_TYPE& val, const size_t w_tid) {
+    view().template warp_insert<skipOverWrites>(key, val, (int)w_tid);
+  }
+  template <bool skipOverWrites = false>
+  __device__ bool warpInsert_V(const KEY_TYPE& key, const VAL_TYPE& val, const size_t w_tid) {
+    return view().template warp_insert<skipOverWrites>(key, val, (int)w_tid);
+  }
+  __device__ void warpFind(const KEY_TYPE& key, VAL_TYPE& val, const size_t w_tid) const {
+    view().warp_find(key, val, (int)w_tid);
+  }
+  __device__ void warpErase(const KEY_TYPE& key, const size_t w_tid) { view().warp_erase(key, (int)w_tid); }
+
+ private:
+  __device__ static const VAL_TYPE& missing_value() {
+    static VAL_TYPE zero = 0;
+    return zero;
+  }
 };
 
 }  // namespace Hashinator

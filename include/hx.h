@@ -124,6 +124,12 @@ hx_status hx_map_destroy(hx_map* map);
 hx_status hx_insert(hx_map* map, const void* d_keys, const void* d_vals, uint64_t n, float target_lf,
                     hx_stream stream);
 
+/* insertIndex(keys, len, targetLF, s) (hashinator.h:1339-1355,
+ * insert_index_kernel kernels_NVIDIA.h:468-612): insert keys[i] with the
+ * value i (its index in this call), same growth rule and upsert as
+ * hx_insert. */
+hx_status hx_insert_index(hx_map* map, const void* d_keys, uint64_t n, float target_lf, hx_stream stream);
+
 /* insert(hash_pair*, size_t, float targetLF = 0.5, stream) (hashinator.h:1359-1374). */
 hx_status hx_insert_pairs(hx_map* map, const void* d_pairs, uint64_t n, float target_lf, hx_stream stream);
 
@@ -168,6 +174,16 @@ hx_status hx_extract_keys(hx_map* map, const hx_pred* pred, void* d_out_keys, ui
  * of 2^new_size_power buckets in one streaming pass; tombstones are dropped.
  * Sets err = success if fill is preserved. */
 hx_status hx_resize(hx_map* map, int new_size_power, hx_stream stream);
+
+/* resize_to_lf(targetLF, targets::device, s) (hashinator.h:530-549): grow
+ * (device rehash) to the smallest size power whose load factor is at most
+ * target_lf; nothing happens when it already is. Synchronises. */
+hx_status hx_resize_to_lf(hx_map* map, float target_lf, hx_stream stream);
+
+/* performCleanupTasks(s) (hashinator.h:643-650): clean_tombstones when
+ * tombstones / buckets > 0.025, then device-rehash to the next size power
+ * while the probe bound exceeds one 32-bucket window. Synchronises. */
+hx_status hx_perform_cleanup_tasks(hx_map* map, hx_stream stream);
 
 /* clear(targets::device, stream) (hashinator.h:492-518): every bucket
  * becomes (EMPTY, 0); fill, tombstones and the probe bound go to zero. */

@@ -61,7 +61,7 @@ struct MapView {
   unsigned int* max_probe;
   int* err;
 
-  static MapView from(const hx_device_view& v) {
+  __host__ __device__ static MapView from(const hx_device_view& v) {
     return MapView{static_cast<Bucket*>(v.buckets), v.size_power, v.fill, v.tombstones, v.max_probe, v.err};
   }
 
@@ -183,8 +183,9 @@ struct MapView {
   // One key per warp: lane l looks at bucket h + i + l of window i, the
   // lowest matching lane wins (the reference's decision rule).
 
-  /* warpInsert (hashinator.h:854): insert or overwrite one key per warp; true
-   * on every lane if the key is new. */
+  /* warpInsert / warpInsert_V (hashinator.h:854, :939): insert or overwrite
+   * one key per warp; true on every lane if the key is new. */
+  template <bool skipOverWrites = false>
   __device__ bool warp_insert(K key, V val, int w_tid) const {
     if (sentinel(key)) return false;
     const uint32_t mask = (1u << size_power) - 1u;
@@ -195,7 +196,7 @@ struct MapView {
       const K k = in ? load_key(b) : Sentinels<K>::TOMB;
       const unsigned match = __ballot_sync(0xffffffffu, in && k == key);
       if (match) {
-        if (w_tid == __ffs(match) - 1) store_value(b, val);
+        if (!skipOverWrites && w_tid == __ffs(match) - 1) store_value(b, val);
         return false;
       }
       unsigned empty = __ballot_sync(0xffffffffu, in && k == Sentinels<K>::EMPTY);
@@ -213,7 +214,7 @@ struct MapView {
               break;
             }
             if (ek == key) {
-              store_value(b, val);
+              if (!skipOverWrites) store_value(b, val);
               res = 2;
               break;
             }

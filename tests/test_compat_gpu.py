@@ -33,3 +33,17 @@ def test_device_api_from_user_kernels(hx, tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
     print(r.stdout[-4000:], r.stderr[-2000:])
     assert r.returncode == 0 and "PASSED" in r.stdout
+
+
+def test_reference_device_api_tests_through_compat_header(hx, tmp_path):
+    """User kernels that take the map's device copy (upload()) and call the
+    element, iterator and warp accessors, as the reference's unit tests do."""
+    from hashinator_gb300 import build
+    exe = tmp_path / "test_compat_device"
+    cmd = [build._nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17", "--extended-lambda",
+           "-I", str(ROOT / "include"), str(ROOT / "tests" / "cpp" / "test_compat_device.cu"), "-o", str(exe),
+           "-L", str(hx.LIB_PATH.parent), "-lhx", f"-Xlinker=-rpath,{hx.LIB_PATH.parent}"]
+    subprocess.run(cmd, check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
+    print(r.stdout[-4000:], r.stderr[-2000:])
+    assert r.returncode == 0 and "PASSED" in r.stdout

@@ -375,3 +375,57 @@ def _filter_buckets(oracle_mod, b, w, op):
         sel = ~sent & (b[homes, 0] != k)
         return b[sel]
     return oracle_mod.copy_if(flat, 2 * w, op).reshape(-1, 2)
+
+
+@pytest.mark.parametrize("w", [4, 8])
+def test_insert_index(hx, oracle_mod, w):
+    """insertIndex: keys[i] -> i, with the reference's growth rule."""
+    dt = _dt(w)
+    keys, _, q, _ = workloads.map_workload(50000, w, 31)
+    m = hx.Hashmap(10, w)  # grows: ceil(log2(50000 / 0.5)) = 17
+    m.insert_index(to_dev(keys))
+    om = oracle_mod.OracleMap(10, w)
+    om.insert(keys, np.arange(len(keys), dtype=dt))
+    inf = m.info()
+    assert inf.size_power == om.info()["size_power"] == 17 and inf.fill == len(keys)
+    k, v, _ = device_mapping(m, w)
+    ok, ov = om.mapping()
+    np.testing.assert_array_equal(k, ok)
+    np.testing.assert_array_equal(v, ov)
+    out = to_dev(np.full(len(q), 0xA5, dt))
+    m.retrieve(to_dev(q), out)
+    want = np.full(len(q), 0xA5, dt)
+    om.retrieve(q, want)
+    np.testing.assert_array_equal(from_dev(out, dt), want)
+
+
+@pytest.mark.parametrize("w", [4, 8])
+def test_resize_to_lf_and_cleanup_tasks(hx, oracle_mod, w):
+    keys, vals, _, e = workloads.map_workload(int(0.9 * (1 << 16)), w, 41, erase_frac=0.1)
+    m = hx.Hashmap(16, w)
+    m.insert(to_dev(keys), to_dev(vals), 0.0)
+    om = oracle_mod.OracleMap(16, w)
+    om.insert(keys, vals, 0.0)
+    m.resize_to_lf(0.95)  # already below: nothing happens
+    assert m.info().size_power == 16
+    # performCleanupTasks: tombstone ratio 0.09 > 0.025 -> clean; probe bound > 32 at LF 0.9 -> grow
+    m.erase(to_dev(e))
+    om.erase(e)
+    assert m.info().max_probe > 32
+    m.perform_cleanup_tasks()
+    inf = m.info()
+    assert inf.tombstone_counter == 0 and inf.max_probe <= 32 and inf.size_power > 16
+    assert inf.current_max_bucket_overflow == 32
+    k, v, _ = device_mapping(m, w)
+    ok, ov = om.mapping()
+    np.testing.assert_array_equal(k, ok)
+    np.testing.assert_array_equal(v, ov)
+    m.resize_to_lf(0.1)
+    sp = 16
+    while inf.fill / (1 << sp) > 0.1:
+        sp += 1
+    inf = m.info()
+    assert inf.size_power == sp and inf.fill == len(ok)
+    k, v, _ = device_mapping(m, w)
+    np.testing.assert_array_equal(k, ok)
+    np.testing.assert_array_equal(v, ov)

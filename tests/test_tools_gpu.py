@@ -122,3 +122,31 @@ def test_copy_if_empty_input(hx):
     import torch
     e = torch.zeros(0, dtype=torch.int32, device="cuda")
     assert hx.tools.copy_if(e, e, hx.Pred.even()) == 0
+
+
+# (x % a) < b is evaluated with a multiply-high remainder in the compaction
+# kernel: check divisors at the edges of the 32-bit range, on u32 elements and
+# on the key / value fields of u32 pairs, against the oracle's plain `%`.
+DIVISORS = [1, 2, 3, 7, 100, 641, 65535, 65536, 65537, 2**31 - 1, 2**31, 2**31 + 11, 2**32 - 2, 2**32 - 1]
+
+
+@pytest.mark.parametrize("a", DIVISORS)
+def test_copy_if_mod_lt_divisors(hx, oracle_mod, a):
+    rng = np.random.default_rng(a)
+    x = rng.integers(0, 2**32, size=200_003, dtype=np.uint64).astype(np.uint32)
+    x[:6] = [0, 1, a - 1 if a > 1 else 0, (a * 3) % 2**32, 2**32 - 1, 2**32 - 2]
+    for b in sorted({1, max(1, a // 2), a - 1 if a > 1 else 1}):
+        out = to_dev(np.zeros(len(x), np.uint32))
+        c = hx.tools.copy_if(to_dev(x), out, hx.Pred.mod_lt(a, b))
+        want = oracle_mod.copy_if(x, 4, oracle_mod.pred(1, 0, a, b))
+        assert c == len(want) == int(((x.astype(np.uint64) % a) < b).sum())
+        np.testing.assert_array_equal(from_dev(out, np.uint32)[:c], want)
+    pairs = rng.integers(0, 2**32, size=2 * 50_001, dtype=np.uint64).astype(np.uint32)
+    pairs[::11] = 2**32 - 1  # EMPTY keys
+    for field, flags in [(hx.FIELD_KEY, 0), (hx.FIELD_VALUE, hx.PRED_SKIP_SENTINELS), (hx.FIELD_VALUE, hx.PRED_NEGATE)]:
+        b = max(1, a // 3)
+        out = to_dev(np.zeros_like(pairs))
+        c = hx.tools.copy_if(to_dev(pairs), out, hx.Pred(hx.PRED_MOD_LT, field, a, b, flags), elem_bytes=8)
+        want = oracle_mod.copy_if(pairs, 8, oracle_mod.pred(1, field, a, b, flags))
+        assert 2 * c == len(want)
+        np.testing.assert_array_equal(from_dev(out, np.uint32)[: 2 * c], want)
