@@ -17,7 +17,10 @@
 // host turns that word into HX_ERR_TIMEOUT.
 #pragma once
 #include "hx_device.cuh"
+#include <mutex>
+#include <set>
 #include <type_traits>
+#include <utility>
 
 namespace hx {
 
@@ -308,17 +311,42 @@ struct CleanArgs {
   unsigned long long* fill;
 };
 
-template <class T, class O, int BLOCK, int R, bool CLEAN, int PK>
+template <class T, int R>
+__device__ __forceinline__ void compact_load(const T* in, uint64_t n, uint64_t chunk, int lane, bool vec,
+                                             T (&x)[R][16 / sizeof(T)]) {
+  constexpr int E = 16 / sizeof(T);
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const uint64_t e = chunk + ((uint64_t)r * 32 + lane) * E;
+    if (vec && e + E <= n) {
+      load_vec<T>(in + e, x[r]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < E; ++q)
+        if (e + q < n) x[r][q] = in[e + q];
+    }
+  }
+}
+
+// One tile = S sub-tiles of BLOCK*R*E elements. The CTA walks its sub-tiles
+// in order, loading sub-tile s+1 while it selects from sub-tile s and stages
+// the selected elements (or their keys) in shared memory at their tile-local
+// output index; one look-back per tile then places the staged run in the
+// output with coalesced stores. Registers hold two sub-tiles whatever S is,
+// and the look-back, which bounds how many tiles per second the GPU can
+// retire, is paid once per S sub-tiles.
+template <class T, class O, int BLOCK, int R, int S, bool CLEAN, int PK>
 __global__ void __launch_bounds__(BLOCK) k_compact(const T* __restrict__ in, O* __restrict__ out, uint64_t n,
                                                   hx_pred pr, uint64_t magic, typename ElemOps<T>::Ctx ctx,
                                                   uint64_t capacity, unsigned long long* d_count, ScanScratch sc,
                                                   bool vec, CleanArgs cl) {
   constexpr int E = ElemOps<T>::E;
   constexpr int WARPS = BLOCK / 32;
-  constexpr uint64_t TILE = (uint64_t)BLOCK * R * E;
+  constexpr uint64_t SUB = (uint64_t)BLOCK * R * E;
+  constexpr uint64_t TILE = SUB * S;
   __shared__ unsigned s_warp[WARPS];
   __shared__ unsigned long long s_tile, s_prefix;
-  __shared__ unsigned s_total;
+  __shared__ unsigned s_sub;
   extern __shared__ __align__(16) unsigned char s_raw[];
   O* s_out = reinterpret_cast<O*>(s_raw);
 
@@ -330,77 +358,84 @@ __global__ void __launch_bounds__(BLOCK) k_compact(const T* __restrict__ in, O* 
   __syncthreads();
   const unsigned long long tile = s_tile;
   const uint64_t tile0 = tile * TILE;
-  const uint64_t chunk = tile0 + (uint64_t)warp * 32 * R * E;
+  const uint64_t wchunk = (uint64_t)warp * 32 * R * E;
 
-  T x[R][E];
-  unsigned f[R];  // selection bits of each held uint4
+  T x[R][E], nx[R][E];
+  compact_load<T, R>(in, n, tile0 + wchunk, lane, vec, x);
+  unsigned staged = 0;  // selected elements of the earlier sub-tiles (block-uniform)
+#pragma unroll 1
+  for (int sub = 0; sub < S; ++sub) {
+    const uint64_t chunk = tile0 + (uint64_t)sub * SUB + wchunk;
+    if (sub + 1 < S) compact_load<T, R>(in, n, chunk + SUB, lane, vec, nx);
+    unsigned f[R];  // selection bits of each held uint4
 #pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const uint64_t e = chunk + ((uint64_t)r * 32 + lane) * E;
-    if (vec && e + E <= n) {
-      load_vec<T>(in + e, x[r]);
-    } else {
-#pragma unroll
-      for (int q = 0; q < E; ++q)
-        if (e + q < n) x[r][q] = in[e + q];
-    }
-    unsigned bits = 0;
-#pragma unroll
-    for (int q = 0; q < E; ++q)
-      if (e + q < n && ElemOps<T>::template pred<PK>(pr, x[r][q], ctx, magic)) bits |= 1u << q;
-    f[r] = bits;
-    if constexpr (CLEAN) {
-      using Tr = PairTraits<T>;
+    for (int r = 0; r < R; ++r) {
+      const uint64_t e = chunk + ((uint64_t)r * 32 + lane) * E;
+      unsigned bits = 0;
 #pragma unroll
       for (int q = 0; q < E; ++q)
-        if (e + q < n && ((bits >> q) & 1u || x[r][q].first == Tr::TOMB)) {
-          T empty;
-          empty.first = Tr::EMPTY;
-          empty.second = 0;
-          const_cast<T*>(in)[e + q] = empty;
-        }
-    }
-  }
-  unsigned pre[R];
-  unsigned acc = 0;
+        if (e + q < n && ElemOps<T>::template pred<PK>(pr, x[r][q], ctx, magic)) bits |= 1u << q;
+      f[r] = bits;
+      if constexpr (CLEAN) {
+        using Tr = PairTraits<T>;
 #pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const unsigned c = __popc(f[r]);
-    const unsigned incl = warp_incl_scan(c, lane);
-    pre[r] = acc + incl - c;
-    acc += __shfl_sync(0xffffffffu, incl, 31);
+        for (int q = 0; q < E; ++q)
+          if (e + q < n && ((bits >> q) & 1u || x[r][q].first == Tr::TOMB)) {
+            T empty;
+            empty.first = Tr::EMPTY;
+            empty.second = 0;
+            const_cast<T*>(in)[e + q] = empty;
+          }
+      }
+    }
+    unsigned pre[R];
+    unsigned acc = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const unsigned c = __popc(f[r]);
+      const unsigned incl = warp_incl_scan(c, lane);
+      pre[r] = acc + incl - c;
+      acc += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (lane == 0) s_warp[warp] = acc;
+    __syncthreads();
+    if (warp == 0) {
+      const unsigned wt = (lane < WARPS) ? s_warp[lane] : 0u;
+      const unsigned wincl = warp_incl_scan(wt, lane);
+      if (lane < WARPS) s_warp[lane] = wincl - wt;
+      if (lane == 31) s_sub = wincl;
+    }
+    __syncthreads();
+    unsigned o = staged + s_warp[warp];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      unsigned p = o + pre[r];
+#pragma unroll
+      for (int q = 0; q < E; ++q)
+        if (f[r] & (1u << q)) s_out[p++] = project<T, O>(x[r][q]);
+    }
+    staged += s_sub;
+    if (sub + 1 < S) {
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int q = 0; q < E; ++q) x[r][q] = nx[r][q];
+    }
+    __syncthreads();  // s_warp and s_sub are rewritten by the next sub-tile
   }
-  if (lane == 0) s_warp[warp] = acc;
-  __syncthreads();
   if (warp == 0) {
-    unsigned wt = (lane < WARPS) ? s_warp[lane] : 0u;
-    const unsigned wincl = warp_incl_scan(wt, lane);
-    const unsigned aggregate = __shfl_sync(0xffffffffu, wincl, 31);
-    const unsigned long long tp = lookback(sc, tile, aggregate, lane);
-    if (lane < WARPS) s_warp[lane] = wincl - wt;
+    const unsigned long long tp = lookback(sc, tile, staged, lane);
     if (lane == 0) {
       s_prefix = tp;
-      s_total = aggregate;
       if (tile0 + TILE >= n) {  // last tile
-        if (d_count) *d_count = tp + aggregate;
-        if constexpr (CLEAN) atomicAdd(cl.fill, 0ull - (tp + aggregate));
+        if (d_count) *d_count = tp + staged;
+        if constexpr (CLEAN) atomicAdd(cl.fill, 0ull - (tp + staged));
       }
     }
   }
   __syncthreads();
-  // Stage selected elements at their tile-local output index.
-  const unsigned wbase = s_warp[warp];
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    unsigned o = wbase + pre[r];
-#pragma unroll
-    for (int q = 0; q < E; ++q)
-      if (f[r] & (1u << q)) s_out[o++] = project<T, O>(x[r][q]);
-  }
-  __syncthreads();
-  const unsigned total = s_total;
   const unsigned long long prefix = s_prefix;
-  for (unsigned i = threadIdx.x; i < total; i += BLOCK) {
+  for (unsigned i = threadIdx.x; i < staged; i += BLOCK) {
     const unsigned long long dst = prefix + i;
     if (dst < capacity) out[dst] = s_out[i];
   }
@@ -410,7 +445,11 @@ __global__ void __launch_bounds__(BLOCK) k_compact(const T* __restrict__ in, O* 
 constexpr int kScanBlock = 256;
 constexpr int kScanR = 12;  // 256 threads x 12 uint4 = 12288 u32 per tile (a sweep of 4..16 peaked here)
 constexpr int kCompactBlock = 256;
-constexpr int kCompactR = 4;  // 256 threads x 4 uint4 = 16 KiB per tile
+constexpr int kCompactR = 4;  // 256 threads x 4 uint4 = 16 KiB per sub-tile
+#ifndef HX_COMPACT_S
+#define HX_COMPACT_S 4
+#endif
+constexpr int kCompactS = HX_COMPACT_S;  // sub-tiles per tile
 
 inline uint64_t scan_tiles(uint64_t n) {
   const uint64_t t = (uint64_t)kScanBlock * kScanR * 4;
@@ -418,7 +457,7 @@ inline uint64_t scan_tiles(uint64_t n) {
 }
 template <class T>
 inline uint64_t compact_tile_elems() {
-  return (uint64_t)kCompactBlock * kCompactR * (16 / sizeof(T));
+  return (uint64_t)kCompactBlock * kCompactR * (16 / sizeof(T)) * kCompactS;
 }
 template <class T>
 inline uint64_t compact_tiles(uint64_t n) {
@@ -434,6 +473,24 @@ inline ScanScratch carve_scratch(void* p, uint64_t tiles) {
   return sc;
 }
 
+// Raise a kernel's dynamic shared-memory limit once (per kernel and device)
+// when it needs more than the default 48 KiB.
+template <class Kern>
+inline cudaError_t allow_dynamic_smem(Kern kern, size_t smem) {
+  if (smem <= 48 * 1024) return cudaSuccess;
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> g(mu);
+  const auto key = std::make_pair(reinterpret_cast<const void*>(kern), dev);
+  if (done.count(key)) return cudaSuccess;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) done.insert(key);
+  return e;
+}
+
 // Launch one compaction pass (n > 0). The scratch must hold
 // scan_scratch_bytes(compact_tiles<T>(n)) bytes; it is zeroed here.
 template <class T, bool CLEAN, class O = T>
@@ -447,34 +504,29 @@ inline cudaError_t launch_compact(const T* in, O* out, uint64_t n, const hx_pred
   const size_t smem = (size_t)compact_tile_elems<T>() * sizeof(O);
   const ScanScratch sc = carve_scratch(scratch, tiles);
   const unsigned grid = (unsigned)tiles;
+  auto launch = [&](auto kern, uint64_t magic) -> cudaError_t {
+    cudaError_t err = allow_dynamic_smem(kern, smem);
+    if (err != cudaSuccess) return err;
+    kern<<<grid, kCompactBlock, smem, s>>>(in, out, n, pr, magic, ctx, capacity, d_count, sc, vec, cl);
+    return cudaGetLastError();
+  };
   if constexpr (CLEAN) {
-    k_compact<T, O, kCompactBlock, kCompactR, true, PK_GENERIC>
-        <<<grid, kCompactBlock, smem, s>>>(in, out, n, pr, 0, ctx, capacity, d_count, sc, vec, cl);
+    return launch(k_compact<T, O, kCompactBlock, kCompactR, kCompactS, true, PK_GENERIC>, 0);
   } else {
-    const int pk = pred_kind<T>(pr);
-    const uint64_t magic = pk == PK_MOD_LT32 ? fastmod_magic((uint32_t)pr.a) : 0;
-    switch (pk) {
+    switch (pred_kind<T>(pr)) {
       case PK_MOD_LT32:
-        k_compact<T, O, kCompactBlock, kCompactR, false, PK_MOD_LT32>
-            <<<grid, kCompactBlock, smem, s>>>(in, out, n, pr, magic, ctx, capacity, d_count, sc, vec, cl);
-        break;
+        return launch(k_compact<T, O, kCompactBlock, kCompactR, kCompactS, false, PK_MOD_LT32>,
+                      fastmod_magic((uint32_t)pr.a));
       case PK_MASK_EQ:
-        k_compact<T, O, kCompactBlock, kCompactR, false, PK_MASK_EQ>
-            <<<grid, kCompactBlock, smem, s>>>(in, out, n, pr, magic, ctx, capacity, d_count, sc, vec, cl);
-        break;
+        return launch(k_compact<T, O, kCompactBlock, kCompactR, kCompactS, false, PK_MASK_EQ>, 0);
       case PK_VALID:
-        if constexpr (!std::is_same<T, uint32_t>::value) {
-          k_compact<T, O, kCompactBlock, kCompactR, false, PK_VALID>
-              <<<grid, kCompactBlock, smem, s>>>(in, out, n, pr, magic, ctx, capacity, d_count, sc, vec, cl);
-          break;
-        }
+        if constexpr (!std::is_same<T, uint32_t>::value)
+          return launch(k_compact<T, O, kCompactBlock, kCompactR, kCompactS, false, PK_VALID>, 0);
         [[fallthrough]];
       default:
-        k_compact<T, O, kCompactBlock, kCompactR, false, PK_GENERIC>
-            <<<grid, kCompactBlock, smem, s>>>(in, out, n, pr, magic, ctx, capacity, d_count, sc, vec, cl);
+        return launch(k_compact<T, O, kCompactBlock, kCompactR, kCompactS, false, PK_GENERIC>, 0);
     }
   }
-  return cudaGetLastError();
 }
 
 }  // namespace hx
