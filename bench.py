@@ -26,6 +26,7 @@ own GPU; value is the sum over ranks).
 from __future__ import annotations
 
 import argparse
+import functools
 import json
 import os
 import subprocess
@@ -128,24 +129,76 @@ def dist_setup():
     return env_ranks()
 
 
-def cpu_baseline(width: int = 4, log_n: int = 24):
-    """Oracle port on a bounded sample: insert + 50/50 query, 1 core."""
-    import oracle
+def _shard_of(keys, sp, shard_bits):
+    """Top shard_bits of each key's home bucket in a table of 2^sp buckets (the Fibonacci hash)."""
+    k = keys.astype(np.uint64)
+    if keys.dtype == np.uint32:
+        k = k ^ (k >> np.uint64(32 - sp))
+        h = (k * np.uint64(2654435769)) >> np.uint64(32 - sp)
+        h &= np.uint64((1 << sp) - 1)
+    else:
+        k = k ^ (k >> np.uint64(64 - sp))
+        h = (k * np.uint64(11400714819323198485)) >> np.uint64(64 - sp)
+    return (h >> np.uint64(sp - shard_bits)).astype(np.int64)
+
+
+@functools.lru_cache(maxsize=4)
+def _cpu_parts(width: int, log_n: int, tb: int):
+    """The CPU sample (keys, values, queries), split into 2^tb shards; generated once per process."""
     from hashinator_gb300 import workloads
+    keys, vals, q, _ = workloads.map_workload(1 << log_n, width, 1234, erase_frac=0.0)
+    if not tb:
+        return [(keys, vals, q)]
+    ks, qs = _shard_of(keys, log_n + 1, tb), _shard_of(q, log_n + 1, tb)
+    return [(np.ascontiguousarray(keys[ks == i]), np.ascontiguousarray(vals[ks == i]),
+             np.ascontiguousarray(q[qs == i])) for i in range(1 << tb)]
+
+
+def cpu_insert_query(width: int = 4, log_n: int = 24, threads: int = 1, reps: int = 1):
+    """The reference's CPU path (the oracle port: serial insert + find) on a bounded sample: 2^log_n keys into
+    2^(log_n+1) buckets, then 2^log_n queries (50% hit). With threads > 1 (a power of two) the host runs one
+    serial map per thread, keys sharded by the top bits of their home bucket, each map a slice of the table at the
+    same load factor; the oracle's calls release the GIL. Returns (Mkeys/s, insert Mkeys/s, query Mkeys/s, s)."""
+    import oracle
+    from concurrent.futures import ThreadPoolExecutor
     n = 1 << log_n
-    keys, vals, q, _ = workloads.map_workload(n, width, 1234, erase_frac=0.0)
-    om = oracle.OracleMap(log_n + 1, width)
-    out = np.zeros(len(q), keys.dtype)
-    t0 = time.perf_counter()
-    om.insert(keys, vals, 0.0)
-    t1 = time.perf_counter()
-    om.retrieve(q, out)
-    t2 = time.perf_counter()
-    total = t2 - t0
-    return {"value": round(2 * n / total / 1e6, 3), "unit": "Mkeys/s", "cores": 1, "kind": "port",
+    tb = max(0, threads.bit_length() - 1)
+    sp = log_n + 1
+    parts = _cpu_parts(width, log_n, tb)
+    outs = [np.zeros(len(p[2]), p[0].dtype) for p in parts]
+    best = None
+    with ThreadPoolExecutor(max_workers=len(parts)) as ex:
+        for _ in range(reps):
+            maps = [oracle.OracleMap(sp - tb, width) for _ in parts]
+            t0 = time.perf_counter()
+            list(ex.map(lambda i: maps[i].insert(parts[i][0], parts[i][1], 0.0), range(len(parts))))
+            t1 = time.perf_counter()
+            list(ex.map(lambda i: maps[i].retrieve(parts[i][2], outs[i]), range(len(parts))))
+            t2 = time.perf_counter()
+            del maps
+            if best is None or t2 - t0 < best[2] - best[0]:
+                best = (t0, t1, t2)
+    t0, t1, t2 = best
+    return 2 * n / (t2 - t0) / 1e6, n / (t1 - t0) / 1e6, n / (t2 - t1) / 1e6, t2 - t0
+
+
+def host_threads() -> int:
+    """Host threads for the CPU baseline: the largest power of two not above the core count."""
+    c = os.cpu_count() or 1
+    return 1 << (c.bit_length() - 1)
+
+
+def cpu_baseline(width: int = 4, log_n: int = 24):
+    """The CPU baseline reported beside the GPU number: all host threads (sharded serial maps) and one core."""
+    t = host_threads()
+    v, vi, vq, secs = cpu_insert_query(width, log_n, t)
+    v1, vi1, vq1, secs1 = cpu_insert_query(width, log_n, 1)
+    return {"value": round(v, 3), "unit": "Mkeys/s", "cores": t, "kind": "port",
             "sample": f"2^{log_n} u32 keys into 2^{log_n + 1} buckets (LF 0.5) + 2^{log_n} queries 50% hit; "
-                      f"insert {n / (t1 - t0) / 1e6:.1f} Mkeys/s, query {n / (t2 - t1) / 1e6:.1f} Mkeys/s",
-            "seconds": round(total, 3)}
+                      f"{t} serial maps (the reference's CPU path restated), keys sharded by the top bits of their "
+                      f"home bucket; insert {vi:.1f} Mkeys/s, query {vq:.1f} Mkeys/s",
+            "single_core": {"value": round(v1, 3), "insert_Mkeys_s": round(vi1, 1), "query_Mkeys_s": round(vq1, 1)},
+            "seconds": round(secs + secs1, 3)}
 
 
 def run_batched(args, stream, dev):
@@ -417,31 +470,26 @@ def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
         return 0
-    import oracle  # the reference's CPU path, restated (no build of the reference exists on this machine)
-    from hashinator_gb300 import workloads
     log_n = 24
     n = 1 << log_n
-    keys, vals, q, _ = workloads.map_workload(n, 4, 1234, erase_frac=0.0)
-    out = np.zeros(len(q), keys.dtype)
+    t = host_threads()
     times = []
     for i in range(args.warmup + args.steps):
-        om = oracle.OracleMap(log_n + 1, 4)
-        t0 = time.perf_counter()
-        om.insert(keys, vals, 0.0)
-        om.retrieve(q, out)
-        dt = time.perf_counter() - t0
-        del om
+        _, _, _, dt = cpu_insert_query(4, log_n, t)
         if i >= args.warmup:
             times.append(dt)
-    t = float(np.mean(times))
-    v = 2 * n / t / 1e6
+    v1, _, _, _ = cpu_insert_query(4, log_n, 1)
+    ms = float(np.mean(times))
+    v = 2 * n / ms / 1e6
+    sample = (f"2^{log_n} u32 keys into 2^{log_n + 1} buckets (LF 0.5) + 2^{log_n} queries 50% hit per step; {t} "
+              f"serial maps (the reference's CPU path, restated in the oracle), keys sharded by the top bits of "
+              f"their home bucket; one core: {v1:.1f} Mkeys/s")
     line = {"impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "Mkeys/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3), "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded bijective keys)",
             "config": {"workload": "single map u32/u32, insert + 50/50 query, LF 0.5",
-                       "sample": f"2^{log_n} keys into 2^{log_n + 1} buckets per step", "parallelism": "none"},
-            "cpu_baseline": {"value": round(v, 3), "unit": "Mkeys/s", "cores": 1, "kind": "port",
-                             "sample": f"2^{log_n} keys, 2^{log_n + 1} buckets, insert + 2^{log_n} queries 50% hit"},
+                       "sample": f"2^{log_n} keys into 2^{log_n + 1} buckets per step", "parallelism": f"{t} threads"},
+            "cpu_baseline": {"value": round(v, 3), "unit": "Mkeys/s", "cores": t, "kind": "port", "sample": sample},
             "e2e": {"value": round(v, 3), "unit": "Mkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0

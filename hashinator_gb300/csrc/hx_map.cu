@@ -409,26 +409,36 @@ static inline bool is_p32(const hx_map* m) { return m->key_bytes == 4; }
 static inline uint64_t pair_bytes(const hx_map* m) { return is_p32(m) ? 8 : 16; }
 static inline uint64_t nslots(const hx_map* m) { return 1ull << m->sp; }
 
-// Automatic probe policy (tune.group == 0), from a GB300 sweep over
-// G x keys-per-thread at load factors 0.5 and 0.9 (2^27 buckets):
-//   insert:       one thread per key, blind home CAS, 1 key per thread;
-//   query/erase:  one thread per key with 4 (u32) or 2 (u64) keys in flight
-//                 below load factor 0.7; 32-lane groups above, where misses
-//                 walk long runs and a 256-512 B window per step wins.
+// Automatic probe policy (tune.group == 0), from GB300 sweeps over
+// G x keys-per-thread at load factors 0.5 - 0.9 (2^27 buckets, u32 and u64):
+//   insert:  one thread per key, blind home CAS, 1 key per thread;
+//   query:   one thread per key with 4 (u32) / 2 (u64) keys in flight below
+//            load factor 0.65, 2 keys (u32) up to 0.85; u64 tables use
+//            16-lane groups from 0.7 and 32-lane groups from 0.8, u32 tables
+//            32-lane groups from 0.85, where misses walk runs of hundreds of
+//            buckets and a 256-512 B window per step wins;
+//   erase:   one thread per key with 2 keys in flight at every load factor
+//            (erased keys are usually present, so a probe ends at the key,
+//            not at the end of a long run; 1.1-2.7x faster than groups).
+enum class Op { INSERT, QUERY, ERASE };
 struct Geo {
   int G, B;
 };
 struct Policy {
   int G, U;
 };
-static Policy auto_policy(const hx_map* m, bool insert) {
-  if (insert) return {1, 1};
+static Policy auto_policy(const hx_map* m, Op op) {
+  if (op == Op::INSERT) return {1, 1};
+  if (op == Op::ERASE) return {1, 2};
   const double lf = (double)m->fill_ub / (double)nslots(m);
-  if (lf < 0.7) return {1, is_p32(m) ? 4 : 2};
-  return {32, 1};
+  const bool p32 = is_p32(m);
+  if (lf < 0.65) return {1, p32 ? 4 : 2};
+  if (p32) return lf < 0.85 ? Policy{1, 2} : Policy{32, 1};
+  if (lf < 0.7) return {1, 2};
+  return lf < 0.8 ? Policy{16, 1} : Policy{32, 1};
 }
-static Policy policy(const hx_map* m, bool insert) {
-  if (m->tune.group == 0) return auto_policy(m, insert);
+static Policy policy(const hx_map* m, Op op) {
+  if (m->tune.group == 0) return auto_policy(m, op);
   return {m->tune.group, m->tune.unroll};
 }
 
@@ -506,7 +516,7 @@ static hx_status launch_insert(hx_map* m, const void* keys, const void* vals, co
                                const unsigned long long* d_n, cudaStream_t s) {
   using K = typename PairTraits<P>::K;
   using V = typename PairTraits<P>::V;
-  const Policy pol = policy(m, true);
+  const Policy pol = policy(m, Op::INSERT);
   const Geo geo = pick_geo(m, pol.G);
   const int block = m->tune.block;
   if (geo.G == 1) {
@@ -559,7 +569,7 @@ template <class P, bool ERASE>
 static hx_status launch_find(hx_map* m, const void* keys, void* vals, void* pairs, uint64_t n, cudaStream_t s) {
   using K = typename PairTraits<P>::K;
   using V = typename PairTraits<P>::V;
-  const Policy pol = policy(m, false);
+  const Policy pol = policy(m, ERASE ? Op::ERASE : Op::QUERY);
   const Geo geo = pick_geo(m, pol.G);
   const int block = m->tune.block;
   if (geo.G == 1) {

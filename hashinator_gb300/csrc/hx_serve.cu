@@ -623,8 +623,12 @@ static hx_status server_step(hx_server* sv, uint32_t* launched) {
     add[r.map] += r.n;
   }
   if (!tasks.empty()) {
-    // chunk the old tables (move) and the new ones (fill) into pieces of 64K buckets
-    constexpr uint64_t kChunk = 1 << 16;
+    // chunk the old tables (move) and the new ones (fill) into pieces of 2048
+    // buckets, 8 per thread: a move is a dependent chain of random CASes per
+    // thread, so small chunks spread one table's rehash over many CTAs
+    // (64K-bucket chunks made a round that grew a few tables run on a handful
+    // of CTAs for hundreds of microseconds)
+    constexpr uint64_t kChunk = 1 << 11;
     std::vector<GrowChunk> fillc, movec;
     for (unsigned i = 0; i < tasks.size(); ++i) {
       const uint64_t nn = 1ull << tasks[i].new_sp;
