@@ -150,3 +150,46 @@ def test_copy_if_mod_lt_divisors(hx, oracle_mod, a):
         want = oracle_mod.copy_if(pairs, 8, oracle_mod.pred(1, field, a, b, flags))
         assert 2 * c == len(want)
         np.testing.assert_array_equal(from_dev(out, np.uint32)[: 2 * c], want)
+
+
+def test_copy_if_concurrent_host_threads_and_streams(hx, oracle_mod):
+    """Arena-backed copy_if from 8 host threads at once, each on its own
+    stream with its own caller scratch and device count (the reference's
+    preallocated.cu: 8 OpenMP threads x 512 vectors): every result equals the
+    oracle's."""
+    import threading
+    import torch
+    rng = np.random.default_rng(8)
+    sizes = [int(s) for s in rng.integers(1, 150_000, size=8 * 24)]
+    data = [rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32) for n in sizes]
+    results = [None] * len(sizes)
+    errors = []
+
+    def worker(t):
+        try:
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                for i in range(t, len(sizes), 8):
+                    n = sizes[i]
+                    x = to_dev(data[i])
+                    out = torch.zeros(n, dtype=torch.int32, device="cuda")
+                    nb = hx.tools.scratch_bytes(hx.SCRATCH_COPY_IF, n)
+                    scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+                    dc = torch.zeros(1, dtype=torch.int64, device="cuda")
+                    hx.tools.copy_if(x, out, hx.Pred.mod_lt(100, 37), scratch=scratch, scratch_bytes=nb, stream=s,
+                                     d_count=dc)
+                    s.synchronize()
+                    c = int(dc.item())
+                    results[i] = out.cpu().numpy().view(np.uint32)[:c]
+        except Exception as e:  # reported below, in the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(t,)) for t in range(8)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
+    for i, x in enumerate(data):
+        want = oracle_mod.copy_if(x, 4, oracle_mod.pred(1, 0, 100, 37))
+        np.testing.assert_array_equal(results[i], want)
