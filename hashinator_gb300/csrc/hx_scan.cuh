@@ -63,9 +63,7 @@ __device__ __forceinline__ unsigned warp_incl_scan(unsigned x, int lane) {
 // (sum of all earlier tiles, modulo 2^62 / 2^32 by caller) and publishes the
 // inclusive prefix. Called by all 32 lanes of warp 0. Each step reads a
 // window of 32 * kLookbackV predecessor statuses (lane l holds distances
-// l*V+1 .. l*V+V) and waits until all of them are published. Wider windows
-// (V = 2, 4, 8) measured slower on GB300 for both scan and compaction: they
-// wait on more of the most recently started tiles.
+// l*V+1 .. l*V+V) and waits for those nearer than the closest inclusive one.
 #ifndef HX_LOOKBACK_V
 #define HX_LOOKBACK_V 1
 #endif
@@ -90,11 +88,24 @@ __device__ __forceinline__ unsigned long long lookback(const ScanScratch& sc, un
       const long long idx = top - (lane * V + j);
       st[j] = (idx >= 0) ? ld_status(sc.status + idx) : kStInc;  // before tile 0: prefix 0
     }
-    // Wait until every status in the window is published.
+    // Wait only for the statuses nearer than the closest inclusive prefix in
+    // the window (all of them if there is none): the ones beyond it are never
+    // summed. Waiting for the whole window meant waiting for the slowest of
+    // 32 neighbours still loading their tiles, which dominated a CTA's life.
     while (true) {
+      int first = V;  // this lane's nearest inclusive status
+#pragma unroll
+      for (int j = V - 1; j >= 0; --j)
+        if ((st[j] >> 62) == 2) first = j;
+      const unsigned inc = __ballot_sync(0xffffffffu, first < V);
+      const int stop_lane = inc ? __ffs(inc) - 1 : 32;
+      const int stop_j = __shfl_sync(0xffffffffu, first, stop_lane & 31);
       bool missing = false;
 #pragma unroll
-      for (int j = 0; j < V; ++j) missing |= (st[j] >> 62) == 0;
+      for (int j = 0; j < V; ++j) {
+        const bool needed = lane < stop_lane || (lane == stop_lane && j <= stop_j);
+        missing |= needed && (st[j] >> 62) == 0;
+      }
       if (!__any_sync(0xffffffffu, missing)) break;
       if (++spins > kSpinLimit) {
         timed_out = true;
