@@ -19,14 +19,13 @@
 
 namespace hx {
 
-constexpr uint64_t kNoAllocTileElems = (uint64_t)kScanBlock * kScanR * 4;
+constexpr uint64_t kNoAllocTileElems = (uint64_t)kScanBlock * kScanTmaR * 4;  // the smaller scan tiles
 constexpr uint64_t kNoAllocTiles = (HX_NOALLOC_SCAN_MAX_N + kNoAllocTileElems - 1) / kNoAllocTileElems;
 static_assert(256 + 8 * kNoAllocTiles <= HX_NOALLOC_SCAN_SCRATCH_BYTES, "ticket/error words + tile statuses fit");
 
 // Look-back scratch of the no-allocation scan: 256 B of ticket and error
-// words, then one 8-byte status word per tile. The array keeps the size the
-// header promises (524,544 B, room for tiles as small as 4096 elements); the
-// scan's tiles of 12,288 elements use at most 175,024 B of it.
+// words, then one 8-byte status word per tile of 4096 elements (524,544 B for
+// the largest scan, 2^28 elements).
 static __device__ __align__(256) unsigned char g_noalloc_scan_scratch[HX_NOALLOC_SCAN_SCRATCH_BYTES];
 
 // Device address of the array, looked up once per device with that device
@@ -68,8 +67,6 @@ extern "C" hx_status hx_exclusive_scan_u32_noalloc(const uint32_t* d_in, uint32_
   const uint64_t tiles = scan_tiles(n);
   // The previous call left its tickets and statuses behind: reset the part used.
   HX_CUDA(cudaMemsetAsync(sc, 0, scan_scratch_bytes(tiles), s));
-  const bool vec = ((uintptr_t)d_in % 16 == 0) && ((uintptr_t)d_out % 16 == 0);
-  k_scan_u32<kScanBlock, kScanR><<<(unsigned)tiles, kScanBlock, 0, s>>>(d_in, d_out, n, carve_scratch(sc, tiles),
-                                                                       vec);
+  HX_CUDA(launch_scan(d_in, d_out, n, sc, s));
   return after_launch();
 }

@@ -210,9 +210,7 @@ hx_status hx_exclusive_scan_u32(const uint32_t* d_in, uint32_t* d_out, uint64_t 
   hx_status st = sc.get(d_scratch, scratch_bytes, scan_scratch_bytes(tiles), s);
   if (st != HX_OK) return st;
   HX_CUDA(cudaMemsetAsync(sc.ptr, 0, scan_scratch_bytes(tiles), s));
-  const bool vec = ((uintptr_t)d_in % 16 == 0) && ((uintptr_t)d_out % 16 == 0);
-  k_scan_u32<kScanBlock, kScanR><<<(unsigned)tiles, kScanBlock, 0, s>>>(d_in, d_out, n, carve_scratch(sc.ptr, tiles),
-                                                                       vec);
+  HX_CUDA(launch_scan(d_in, d_out, n, sc.ptr, s));
   return after_launch();
 }
 
