@@ -19,6 +19,7 @@
 #include "hx_device.cuh"
 #include <mutex>
 #include <set>
+#include <atomic>
 #include <type_traits>
 #include <utility>
 
@@ -680,16 +681,16 @@ inline cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint64_t n, vo
   if (((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0) {
     auto kern = k_scan_u32_tma<kScanBlock, kScanTmaR>;
     constexpr size_t smem = 2ull * kScanBlock * kScanTmaR * 16;
-    static int blocks_per_sm[64] = {0};
+    static std::atomic<int> blocks_per_sm[64];  // occupancy per device, 0 until first queried
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    int per_sm = dev < 64 ? blocks_per_sm[dev] : 0;
+    int per_sm = dev < 64 ? blocks_per_sm[dev].load(std::memory_order_relaxed) : 0;
     if (per_sm == 0) {
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kScanBlock, smem);
       if (e != cudaSuccess) return e;
       if (per_sm < 1) per_sm = 1;
-      if (dev < 64) blocks_per_sm[dev] = per_sm;  // a benign race: every writer stores the same value
+      if (dev < 64) blocks_per_sm[dev].store(per_sm, std::memory_order_relaxed);  // every writer stores the same
     }
     int sms = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
