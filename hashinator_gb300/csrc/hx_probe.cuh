@@ -177,6 +177,60 @@ __device__ __forceinline__ int probe_find(const P* __restrict__ table, int sp, t
 }
 
 
+// probe_find with a single exit at the top of the step loop (a key stays
+// "live" until a match, an EMPTY bucket or the probe bound ends it). For u32
+// tables this form measured 6-49% faster than probe_find for 4- and 8-lane
+// groups at load factor 0.5-0.9 on GB300, and slower for u64 tables, so u32
+// queries use it. Returns the lane of the group that found the key (value in
+// val on that lane) or -1.
+template <class P, int G, int B>
+__device__ __forceinline__ int probe_find_live(const P* __restrict__ table, int sp, typename PairTraits<P>::K key,
+                                               bool act, unsigned limit, int lane, unsigned gmask,
+                                               typename PairTraits<P>::V& val) {
+  using K = typename PairTraits<P>::K;
+  using V = typename PairTraits<P>::V;
+  constexpr K EMPTY = PairTraits<P>::EMPTY;
+  constexpr int W = G * B;
+  const int glane = lane & (G - 1);
+  const uint32_t tmask = (1u << sp) - 1u;
+  const uint32_t h = act ? home_slot(key, sp) : 0u;
+  const uint32_t wstart = h & ~(uint32_t)(W - 1);
+  const int first = (int)(h - wstart);
+  bool live = act;
+  int who = -1;
+  for (uint32_t s = 0;; ++s) {
+    K kk[B];
+    V vv[B];
+    const long long d0 = (long long)s * W - first;
+    if (live && d0 >= (long long)limit) live = false;  // past the probe bound: a miss
+    const uint32_t b0 = ((wstart + s * (uint32_t)W) & tmask) + glane * B;
+    if (!live) return who;  // the same on every lane of the group
+    load_buckets<B>(table + b0, kk, vv);
+    unsigned mbits = 0, ebits = 0;
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const long long d = d0 + glane * B + j;
+      const bool cons = d >= 0 && d < (long long)limit;
+      if (cons && kk[j] == key) mbits |= 1u << j;
+      if (cons && kk[j] == EMPTY) ebits |= 1u << j;
+    }
+    const unsigned gm = group_ballot<G>(gmask, lane, mbits != 0);
+    if (gm) {
+      const int w = __ffs(gm) - 1;
+      if (glane == w) {
+        const int j = __ffs(mbits) - 1;
+#pragma unroll
+        for (int t = 0; t < B; ++t)
+          if (t == j) val = vv[t];
+      }
+      who = w;
+      live = false;
+    } else if (group_ballot<G>(gmask, lane, ebits != 0)) {
+      live = false;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Thread-per-key probing (probe group of one lane): a thread holds U keys
 // and issues all their first-window loads (or, for insert, their home-bucket
