@@ -153,42 +153,20 @@ __global__ void __launch_bounds__(BLOCK, HX_BATCH_MIN_WARPS * 32 / BLOCK > 0 ? H
             count = begin < nm ? (nm - begin < count ? nm - begin : count) : 0;
             src = a.moved + a.moved_off[map];
           }
-          if (!groups) {
-            for (unsigned k = threadIdx.x; k < count; k += BLOCK) {
-              K key;
-              V val;
-              if (src) {
-                const P pr = src[begin + k];
-                key = pr.first;
-                val = pr.second;
-              } else {
-                key = a.ins_keys[begin + k];
-                val = a.ins_vals[begin + k];
-              }
-              insert_one_t1<P, BT>(tab, sp, key, val, ins, maxd, fail);
+          // inserts are thread-per-key whatever the tuned group width: on
+          // GB300 they measured fastest at every load factor
+          for (unsigned k = threadIdx.x; k < count; k += BLOCK) {
+            K key;
+            V val;
+            if (src) {
+              const P pr = src[begin + k];
+              key = pr.first;
+              val = pr.second;
+            } else {
+              key = a.ins_keys[begin + k];
+              val = a.ins_vals[begin + k];
             }
-          } else if constexpr (G > 1) {
-            const unsigned gmask = group_mask<G>(lane);
-            for (unsigned k = threadIdx.x / G; k < count; k += BLOCK / G) {
-              K key;
-              V val;
-              if (src) {
-                const P pr = src[begin + k];
-                key = pr.first;
-                val = pr.second;
-              } else {
-                key = a.ins_keys[begin + k];
-                val = a.ins_vals[begin + k];
-              }
-              if (key == EMPTY || key == TOMB) continue;
-              unsigned d1 = 0;
-              const int r = probe_insert<P, G, BG>(tab, sp, key, val, lane, gmask, d1);
-              if (d1) {
-                ++ins;
-                maxd = d1 > maxd ? d1 : maxd;
-              }
-              if (r == PR_FAIL && (lane & (G - 1)) == 0) fail = true;
-            }
+            insert_one_t1<P, BT>(tab, sp, key, val, ins, maxd, fail);
           }
           break;
         }
@@ -198,7 +176,8 @@ __global__ void __launch_bounds__(BLOCK, HX_BATCH_MIN_WARPS * 32 / BLOCK > 0 ? H
           const K* keys = erase ? a.e_keys : a.q_keys;
           const unsigned limit = inf->max_probe;
           if (limit == 0) break;
-          if (!groups) {
+          // the tuned group width applies to queries; erases are thread-per-key
+          if (!groups || erase) {
             for (unsigned base = 0; base < t.count; base += BLOCK * U) {
               K key[U];
               bool act[U];
@@ -238,14 +217,10 @@ __global__ void __launch_bounds__(BLOCK, HX_BATCH_MIN_WARPS * 32 / BLOCK > 0 ? H
               if (key == EMPTY || key == TOMB) continue;
               uint32_t slot;
               V v;
-              const int w = probe_find<P, G, BG>(tab, sp, key, limit, lane, gmask, slot, v);
-              if (w >= 0 && (lane & (G - 1)) == w) {
-                if (erase) {
-                  if (cas_key(tab + slot, key, TOMB)) ++erased;
-                } else {
-                  a.q_out[t.begin + k] = v;
-                }
-              }
+              int w;
+              if constexpr (sizeof(P) == 8) w = probe_find_live<P, G, BG>(tab, sp, key, true, limit, lane, gmask, v);
+              else w = probe_find<P, G, BG>(tab, sp, key, limit, lane, gmask, slot, v);
+              if (w >= 0 && (lane & (G - 1)) == w) a.q_out[t.begin + k] = v;
             }
           }
           break;
