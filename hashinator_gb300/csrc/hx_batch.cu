@@ -215,11 +215,8 @@ __global__ void __launch_bounds__(BLOCK, HX_BATCH_MIN_WARPS * 32 / BLOCK > 0 ? H
             for (unsigned k = threadIdx.x / G; k < t.count; k += BLOCK / G) {
               const K key = keys[t.begin + k];
               if (key == EMPTY || key == TOMB) continue;
-              uint32_t slot;
               V v;
-              int w;
-              if constexpr (sizeof(P) == 8) w = probe_find_live<P, G, BG>(tab, sp, key, true, limit, lane, gmask, v);
-              else w = probe_find<P, G, BG>(tab, sp, key, limit, lane, gmask, slot, v);
+              const int w = probe_find_live<P, G, BG>(tab, sp, key, true, limit, lane, gmask, v);
               if (w >= 0 && (lane & (G - 1)) == w) a.q_out[t.begin + k] = v;
             }
           }

@@ -140,11 +140,8 @@ __global__ void __launch_bounds__(256) k_retrieve(const typename PairTraits<P>::
       if constexpr (PAIRS) key = pairs[i].first;
       else key = keys[i];
       if (key != PairTraits<P>::EMPTY && key != PairTraits<P>::TOMB) {
-        uint32_t slot;
         V v;
-        int w;
-        if constexpr (sizeof(P) == 8) w = probe_find_live<P, G, B>(table, sp, key, true, limit, lane, gmask, v);  // u32
-        else w = probe_find<P, G, B>(table, sp, key, limit, lane, gmask, slot, v);
+        const int w = probe_find_live<P, G, B>(table, sp, key, true, limit, lane, gmask, v);
         if (w >= 0 && (lane & (G - 1)) == w) {
           if constexpr (PAIRS) pairs[i].second = v;
           else vals[i] = v;
@@ -414,12 +411,12 @@ static inline uint64_t nslots(const hx_map* m) { return 1ull << m->sp; }
 // Automatic probe policy (tune.group == 0), from GB300 sweeps over
 // G x keys-per-thread at load factors 0.5 - 0.9 (2^27 buckets, u32 and u64):
 //   insert:  one thread per key, blind home CAS, 1 key per thread;
-//   query:   u32 tables: 4-lane groups (one 32 B sector per step) below
-//            load factor 0.875, 8-lane groups above (31.6 vs 29.8 G keys/s
-//            for thread-per-key at 0.5, 7.9 vs 6.7 for 32 lanes at 0.9);
-//            u64 tables: one thread per key with 2 keys in flight below 0.7,
-//            16-lane groups to 0.8, 32-lane groups above, where misses walk
-//            runs of hundreds of buckets and a 512 B window per step wins;
+//   query:   probe groups with the single-exit probe loop: u32 tables use
+//            4 lanes (64 B windows) below load factor 0.875 and 8 above (31.6
+//            vs 29.8 G keys/s for thread-per-key at 0.5, 7.9 vs 6.7 for 32
+//            lanes at 0.9); u64 tables 4 lanes below 0.8, 8 to 0.875, 16 above
+//            (24.8 vs 21.1 G keys/s for thread-per-key at 0.5, 12.9 vs 10.6 for
+//            16 lanes at 0.75);
 //   erase:   one thread per key with 2 keys in flight at every load factor
 //            (erased keys are usually present, so a probe ends at the key,
 //            not at the end of a long run; 1.1-2.7x faster than groups).
@@ -436,9 +433,8 @@ static Policy auto_policy(const hx_map* m, Op op) {
   const double lf = (double)m->fill_ub / (double)nslots(m);
   const bool p32 = is_p32(m);
   if (p32) return lf < 0.875 ? Policy{4, 1} : Policy{8, 1};
-  if (lf < 0.65) return {1, 2};
-  if (lf < 0.7) return {1, 2};
-  return lf < 0.8 ? Policy{16, 1} : Policy{32, 1};
+  if (lf < 0.8) return {4, 1};
+  return lf < 0.875 ? Policy{8, 1} : Policy{16, 1};
 }
 static Policy policy(const hx_map* m, Op op) {
   if (m->tune.group == 0) return auto_policy(m, op);

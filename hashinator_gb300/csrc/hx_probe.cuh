@@ -178,11 +178,11 @@ __device__ __forceinline__ int probe_find(const P* __restrict__ table, int sp, t
 
 
 // probe_find with a single exit at the top of the step loop (a key stays
-// "live" until a match, an EMPTY bucket or the probe bound ends it). For u32
-// tables this form measured 6-49% faster than probe_find for 4- and 8-lane
-// groups at load factor 0.5-0.9 on GB300, and slower for u64 tables, so u32
-// queries use it. Returns the lane of the group that found the key (value in
-// val on that lane) or -1.
+// "live" until a match, an EMPTY bucket or the probe bound ends it). For 4-
+// and 8-lane groups this form measured 6-49% faster than probe_find at load
+// factor 0.5-0.9 on GB300 (u32 and u64 tables), which made small groups the
+// fastest queries; the group query kernels use it. Returns the lane of the
+// group that found the key (value in val on that lane) or -1.
 template <class P, int G, int B>
 __device__ __forceinline__ int probe_find_live(const P* __restrict__ table, int sp, typename PairTraits<P>::K key,
                                                bool act, unsigned limit, int lane, unsigned gmask,
