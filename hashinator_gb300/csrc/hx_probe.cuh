@@ -130,6 +130,84 @@ __device__ __forceinline__ int probe_insert(P* __restrict__ table, int sp, typen
   }
 }
 
+// probe_insert with a single exit at the top of the step loop (the form the
+// group insert kernel uses; at load factor 0.9 it measured 4-15% faster than
+// probe_insert for 2-8-lane groups on GB300).
+template <class P, int G, int B>
+__device__ __forceinline__ int probe_insert_live(P* __restrict__ table, int sp, typename PairTraits<P>::K key,
+                                                 typename PairTraits<P>::V val, int lane, unsigned gmask,
+                                                 unsigned& dist1) {
+  using K = typename PairTraits<P>::K;
+  using V = typename PairTraits<P>::V;
+  constexpr K EMPTY = PairTraits<P>::EMPTY;
+  constexpr int W = G * B;
+  const int glane = lane & (G - 1);
+  const uint32_t tmask = (1u << sp) - 1u;
+  const long long tsize = (long long)tmask + 1;
+  const uint32_t h = home_slot(key, sp);
+  const uint32_t wstart = h & ~(uint32_t)(W - 1);
+  const int first = (int)(h - wstart);
+  int res = PR_CONTINUE;
+  for (uint32_t s = 0;; ++s) {
+    const long long d0 = (long long)s * W - first;
+    if (res == PR_CONTINUE && d0 >= tsize) res = PR_FAIL;
+    if (res != PR_CONTINUE) return res;  // the same on every lane of the group
+    P* wp = table + ((wstart + s * (uint32_t)W) & tmask) + glane * B;
+    K kk[B];
+    V vv[B];
+    load_buckets<B>(wp, kk, vv);
+    unsigned mbits = 0, ebits = 0;
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const long long d = d0 + glane * B + j;
+      const bool cons = d >= 0 && d < tsize;
+      if (cons && kk[j] == key) mbits |= 1u << j;
+      if (cons && kk[j] == EMPTY) ebits |= 1u << j;
+    }
+    const unsigned gm = group_ballot<G>(gmask, lane, mbits != 0);
+    if (gm) {
+      if (glane == __ffs(gm) - 1) store_value(wp + (__ffs(mbits) - 1), val);
+      res = PR_UPDATED;
+      continue;
+    }
+    unsigned ge = group_ballot<G>(gmask, lane, ebits != 0);
+    while (ge) {
+      const int w = __ffs(ge) - 1;
+      int r = PR_CONTINUE;
+      if (glane == w) {
+        const int j = __ffs(ebits) - 1;
+        K ek = EMPTY;
+        V ev = 0;
+#pragma unroll
+        for (int t = 0; t < B; ++t)
+          if (t == j) ev = vv[t];
+        for (int tries = 0;; ++tries) {
+          if (cas_pair(wp + j, ek, ev, key, val)) {
+            r = PR_INSERTED;
+            dist1 = (unsigned)(d0 + glane * B + j) + 1u;
+            break;
+          }
+          if (ek == key) {
+            store_value(wp + j, val);
+            r = PR_UPDATED;
+            break;
+          }
+          if (ek != EMPTY || tries >= 8) {
+            ebits &= ~(1u << j);
+            break;
+          }
+        }
+      }
+      r = group_shfl<G>(gmask, r, w);
+      if (r != PR_CONTINUE) {
+        res = r;
+        break;
+      }
+      ge = group_ballot<G>(gmask, lane, ebits != 0);
+    }
+  }
+}
+
 // Find one key within `limit` buckets of its home. Returns the group lane
 // holding it (its bucket index in `slot`, value in `val`) or -1.
 template <class P, int G, int B>
