@@ -229,8 +229,11 @@ __global__ void __launch_bounds__(BLOCK) k_scan_u32(const uint32_t* in, uint32_t
 // Persistent CTAs take tickets in order and finish their tiles in order; a
 // tile's aggregate depends only on its CTA's own copy and on look-backs of
 // lower tiles, so the lowest unpublished tile can always progress. Every wait
-// is bounded: an mbarrier wait gives up after about a second and records an
-// error (later waits of that CTA are then skipped).
+// is bounded: an mbarrier wait gives up after about a second; the CTA then
+// stops taking tiles at the end of that iteration, waits once more (bounded)
+// for each bulk copy it issued that has not completed, records the error and
+// returns. Tiles it never published are resolved by the bounded look-back of
+// later tiles, which record the error too.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
@@ -285,6 +288,9 @@ __global__ void __launch_bounds__(BLOCK) k_scan_u32_tma(const uint32_t* in, uint
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned long long tiles = (n + TILE - 1) / TILE;
   const unsigned long long full_tiles = n / TILE;
+  // Per stage s, bit s of: par = parity of the next wait on its barrier;
+  // pend = a fill was issued that this thread has not yet seen complete.
+  unsigned par = 0, pend = 0;
   // Fill stage st with tile t: a full tile by one bulk copy, the ragged last
   // tile by plain loads (zero beyond n). Called by all threads.
   auto fill = [&](int st, unsigned long long t) {
@@ -302,6 +308,7 @@ __global__ void __launch_bounds__(BLOCK) k_scan_u32_tma(const uint32_t* in, uint
       __syncthreads();
       if (threadIdx.x == 0) mbar_arrive_expect_tx(&s_bar[st], 0);
     }
+    pend |= 1u << st;
   };
   if (threadIdx.x == 0) {
     mbar_init(&s_bar[0], 1);
@@ -315,11 +322,16 @@ __global__ void __launch_bounds__(BLOCK) k_scan_u32_tma(const uint32_t* in, uint
   if (cur >= tiles) return;
   fill(0, cur);
   if (nxt < tiles) fill(1, nxt);
-  unsigned phase[2] = {0, 0};
-  bool ok = true;
+  bool ok = true, failed = false;
   // Per-warp totals of the tile in stage st, and its aggregate published.
   auto reduce = [&](int st, unsigned long long t) {
-    ok = ok && mbar_wait_bounded(&s_bar[st], phase[st]);
+    if (ok) {
+      ok = mbar_wait_bounded(&s_bar[st], (par >> st) & 1u);
+      if (ok) {
+        par ^= 1u << st;
+        pend &= ~(1u << st);
+      }
+    }
     const uint4* b = s_buf + (size_t)st * (TILE / 4) + warp * 32 * R;
     unsigned acc = 0;
 #pragma unroll
@@ -373,9 +385,8 @@ __global__ void __launch_bounds__(BLOCK) k_scan_u32_tma(const uint32_t* in, uint
         }
       }
     }
-    phase[st] ^= 1;
-    __syncthreads();  // stage st and its totals are free
-    if (nxt >= tiles) break;
+    failed = __syncthreads_or(!ok);  // stage st and its totals are free
+    if (failed || nxt >= tiles) break;
     if (threadIdx.x == 0) s_tile[st] = atomicAdd(sc.ticket, 1u);
     __syncthreads();
     const unsigned long long after = s_tile[st];
@@ -384,7 +395,13 @@ __global__ void __launch_bounds__(BLOCK) k_scan_u32_tma(const uint32_t* in, uint
     nxt = after;
     st ^= 1;
   }
-  if (!ok && threadIdx.x == 0) atomicExch(sc.error, 1u);
+  if (failed && threadIdx.x == 0) {
+    // No fill follows a failed wait, so each stage has at most one copy
+    // outstanding; give each one more bounded wait before the CTA exits.
+    for (int s = 0; s < 2; ++s)
+      if ((pend >> s) & 1u) mbar_wait_bounded(&s_bar[s], (par >> s) & 1u);
+    atomicExch(sc.error, 1u);
+  }
 }
 
 // ---------------------------------------------------------------------------
