@@ -224,9 +224,10 @@ hx_status hx_map_device_view(hx_map* map, hx_device_view* out);
  * keys_per_thread in {1,2,4,8} keys in flight), applied to insert, retrieve
  * and erase alike; block_size a multiple of 32 up to 256. 0 keeps the
  * current value. Until a group width is set, each call picks its own: one
- * thread per key for insert and erase, small probe groups for retrieve
- * (u32: 4 lanes below load factor 0.875, 8 above; u64: 4 below 0.8, 8 to
- * 0.875, 16 above). */
+ * thread per key for erase, for the re-insert of clean_tombstones and for
+ * an insert whose load factor ends below 0.85 (4-lane groups above); small
+ * probe groups for retrieve (u32: 4 lanes below load factor 0.875, 8 above;
+ * u64: 4 below 0.8, 8 to 0.875, 16 above). */
 hx_status hx_map_set_tuning(hx_map* map, int group_width, int keys_per_thread, int block_size);
 
 /* Thread-per-key insert mode (no reference counterpart): blind_cas != 0
