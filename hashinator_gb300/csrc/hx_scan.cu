@@ -102,7 +102,7 @@ static hx_status copy_if_t(const void* d_in, void* d_out, uint64_t n, const hx_p
 
 // Random 32-byte sector reads over a buffer of 2^k sectors: the random-access
 // ceiling of the memory system, against which the probe kernels (one random
-// sector per key at least) are judged. U independent reads per thread.
+// sector per key at least) are measured. U independent reads per thread.
 __device__ __forceinline__ uint64_t diag_mix(uint64_t i) {
   uint64_t x = i * 0x9E3779B97F4A7C15ull;
   x ^= x >> 29;

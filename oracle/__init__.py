@@ -3,7 +3,7 @@
 A serial CPU restatement of the Hashinator hot path (oracle/hx_oracle.c,
 compiled into oracle/liboracle.so) with numpy bindings. Only tests/,
 __graft_entry__.smoke() and bench.py's CPU-baseline / reference legs use it,
-always as the checker or the timed CPU baseline, never as the product path.
+always as the parity oracle or the timed CPU baseline, never as the product path.
 
 Pinning: tests/test_oracle_golden.py checks this oracle against golden
 fixtures produced by the reference's own CPU-only build

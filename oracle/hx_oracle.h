@@ -1,6 +1,6 @@
 /*
  * hx_oracle.h — TEST INFRASTRUCTURE ONLY. A serial CPU restatement of the
- * Hashinator hot path used as the parity checker for libhx. Nothing in the
+ * Hashinator hot path used as the parity oracle for libhx. Nothing in the
  * product links or calls it; only tests/, __graft_entry__.smoke() and the
  * CPU-baseline leg of bench.py do.
  *

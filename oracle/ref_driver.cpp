@@ -8,7 +8,7 @@
 // Input (little-endian u64 header, then arrays of key_bytes-wide words):
 //   magic 0x48584752, key_bytes, size_power, n_ins, n_q, n_e, fill_pattern
 //   keys[n_ins] vals[n_ins] qkeys[n_q] ekeys[n_e]
-// Operations (CPU-only API, SURVEY-documented quirks avoided):
+// Operations (the reference's CPU-only API):
 //   Hashmap<K,K> m(size_power); m.insert(keys, vals, n_ins)  [serial _at]
 //   query 1: find(q) for every q (hit -> value, miss -> fill_pattern)
 //   erase(e) for every e, summing the returned counts
