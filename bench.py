@@ -43,6 +43,20 @@ sys.path.insert(0, str(ROOT))
 INSERT_BYTES_PER_KEY = {4: 72, 8: 80}
 QUERY_BYTES_PER_KEY = {4: 40, 8: 48}
 METRIC = "insert+query Mkeys/s (u32 keys/values, 2^26 keys, 2^27 buckets, LF 0.5, 50% hit queries)"
+DATA = "synthetic (seeded bijective keys, PCG64 values)"
+
+
+def headline_metric(log_keys: int) -> str:
+    """The headline metric string for 2^log_keys keys in 2^(log_keys+1) buckets."""
+    return METRIC if log_keys == 26 else METRIC.replace("2^26 keys, 2^27", f"2^{log_keys} keys, 2^{log_keys + 1}")
+
+
+def headline_config(log_keys: int, group: int) -> dict:
+    """The headline workload's config; both arms report it."""
+    return {"workload": f"single map u32/u32: clear + insert 2^{log_keys} + retrieve 2^{log_keys} (50% hit)",
+            "size_power": log_keys + 1, "keys": 1 << log_keys, "load_factor": 0.5, "parallelism": "replicas",
+            "l2": "inputs larger than L2 (1 GiB table, 256 MiB arrays); no flush",
+            "group_width": group or "default"}
 
 
 def measured_peak():
@@ -487,11 +501,13 @@ def run_reference(args):
     sample = (f"2^{log_n} u32 keys into 2^{log_n + 1} buckets (LF 0.5) + 2^{log_n} queries 50% hit per step; {t} "
               f"serial maps (the reference's CPU path, restated in the oracle), keys sharded by the top bits of "
               f"their home bucket; one core: {v1:.1f} Mkeys/s")
-    line = {"impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "Mkeys/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms * 1e3, 3), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded bijective keys)",
-            "config": {"workload": "single map u32/u32, insert + 50/50 query, LF 0.5",
-                       "sample": f"2^{log_n} keys into 2^{log_n + 1} buckets per step", "parallelism": f"{t} threads"},
+    config = headline_config(args.log_keys, args.group)
+    config.update({"reference_sample": f"2^{log_n} keys into 2^{log_n + 1} buckets per step",
+                   "reference_host_threads": t})
+    line = {"impl": "reference", "metric": headline_metric(args.log_keys), "value": round(v, 3), "unit": "Mkeys/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": DATA,
+            "config": config,
             "cpu_baseline": {"value": round(v, 3), "unit": "Mkeys/s", "cores": t, "kind": "port", "sample": sample},
             "e2e": {"value": round(v, 3), "unit": "Mkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -729,16 +745,10 @@ def run_ours(args):
         streaming = run_streaming(args, stream, dev, peak)
 
     if rank == 0:
-        metric = METRIC if args.log_keys == 26 else METRIC.replace("2^26 keys, 2^27", f"2^{args.log_keys} keys, 2^{sp}")
-        line = {"metric": metric, "value": round(value, 3), "unit": "Mkeys/s", "n_gpus": world,
+        line = {"metric": headline_metric(args.log_keys), "value": round(value, 3), "unit": "Mkeys/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-                "data": "synthetic (seeded bijective keys, PCG64 values)",
-                "config": {"workload": f"single map u32/u32: clear + insert 2^{args.log_keys} + retrieve "
-                                       f"2^{args.log_keys} (50% hit)",
-                           "size_power": sp, "keys": n, "load_factor": 0.5, "parallelism": "replicas",
-                           "l2": "inputs larger than L2 (1 GiB table, 256 MiB arrays); no flush",
-                           "group_width": args.group or "default"},
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": DATA,
+                "config": headline_config(args.log_keys, args.group),
                 "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
                 "batched": batched, "serving": serving, "large_map_lf_sweep": lf_sweep, "streaming": streaming,
                 "clocks": clocks}
