@@ -166,12 +166,10 @@ def batched_workload(n_maps: int, seed: int, log_lo: float = 6.0, log_hi: float 
     hits = keys[kstart[hseg] + (c[hseg] * hj + d[hseg]) % n[hseg]]
     nq = n_hit + n_miss
     qseg, qj, qstart = _segments(nq)
-    src = np.where(qj < n_hit[qseg], 0, 1)
     vals_q = np.empty(len(qj), np.uint32)
     hit_pos = qj < n_hit[qseg]
     vals_q[hit_pos] = hits
     vals_q[~hit_pos] = misses
-    del src
     e_mul = _coprime(rng, nq)
     f_add = rng.integers(0, np.maximum(nq, 1))
     queries = np.empty_like(vals_q)
@@ -199,7 +197,9 @@ def serving_trace(n_maps: int, n_requests: int, seed: int, init_log=(8.0, 20.0),
     2^U keys (U ~ U[size_log], at least 1), op insert/query/erase with probabilities `mix`. Inserts bring
     fresh keys; queries draw `present` of their keys from keys inserted so far and the rest fresh
     (absent); erases draw from keys inserted so far. Map i's keys are positions [i*2^40, ...) of one
-    bijective key stream, so maps never share keys. Returns a dict of flat host arrays."""
+    bijective key stream, so with 8-byte keys maps never share keys; with 4-byte keys the positions wrap
+    at 2^32 and maps may share keys (each map is a separate table, so that changes no result). The keys
+    inserted into one map are distinct. Returns a dict of flat host arrays."""
     rng = np.random.default_rng(seed)
     n0 = np.rint(2.0 ** rng.uniform(init_log[0], init_log[1], size=n_maps)).astype(np.int64)
     sp = np.maximum(np.ceil(np.log2(n0 / init_lf)), 2).astype(np.int32)
