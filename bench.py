@@ -15,8 +15,11 @@ roofline: the dominant kernel's algorithmic bytes (insert 72 B/key, query
        40 B/key: key+value in, one 32 B bucket sector read, written back for
        insert) over its event-timed duration, against the measured HBM copy
        bandwidth (MEASURED_PEAKS.json).
-cpu_baseline: the oracle's serial C restatement on a bounded sample
-       (2^24 keys into 2^25 buckets, same load factor), one host core.
+cpu_baseline: the oracle's serial C restatement of the reference's CPU path on
+       a bounded sample (2^24 keys into 2^25 buckets, same load factor), as
+       one serial map per host thread (keys sharded by home bucket) and on one
+       core; beside it, the streaming primitives on 2^24 u32 (one core and all
+       host threads).
 
 --impl reference times the reference's CPU implementation of the path (the
 oracle port of it on this machine) on the same metric.
@@ -212,7 +215,85 @@ def cpu_baseline(width: int = 4, log_n: int = 24):
                       f"{t} serial maps (the reference's CPU path restated), keys sharded by the top bits of their "
                       f"home bucket; insert {vi:.1f} Mkeys/s, query {vq:.1f} Mkeys/s",
             "single_core": {"value": round(v1, 3), "insert_Mkeys_s": round(vi1, 1), "query_Mkeys_s": round(vq1, 1)},
-            "seconds": round(secs + secs1, 3)}
+            "seconds": round(secs + secs1, 3), "streaming": _guarded(cpu_streaming)}
+
+
+def _guarded(fn):
+    """fn() or, if it raises, a record of the error (an optional section never ends the run)."""
+    try:
+        return fn()
+    except Exception as e:  # noqa: BLE001
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
+def cpu_streaming(log_n: int = 24, threads: int | None = None, reps: int = 3) -> dict:
+    """CPU baseline of the streaming primitives on a bounded sample of 2^log_n u32 (uniform; scan input in
+    [0, 16)): the oracle's serial copy_if with (x % 100) < s, s = 1/50/99, and its serial exclusive scan, on one
+    core and as two-pass chunked versions on `threads` host threads (chunk results, then chunk offsets, then a
+    parallel placement; the oracle's calls and numpy's copies release the GIL). The reference has no CPU code for
+    these (split::tools is device-only), so this restates them. Rates in G elements/s and GB/s of the same
+    algorithmic bytes as the GPU figures (copy_if 4 B per element + 4 B per selected; scan 8 B per element)."""
+    import ctypes
+    import oracle
+    from concurrent.futures import ThreadPoolExecutor
+    t = threads or host_threads()
+    n = 1 << log_n
+    rng = np.random.default_rng(28)
+    x = rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
+    xs = rng.integers(0, 16, size=n, dtype=np.uint32)
+    bounds = [(i * n // t, (i + 1) * n // t) for i in range(t)]
+    lib = oracle.lib()
+
+    def best_of(fn):
+        best = None
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            r = fn()
+            dt = time.perf_counter() - t0
+            if best is None or dt < best[0]:
+                best = (dt, r)
+        return best
+
+    def rates(dt, nbytes):
+        return {"ms": round(dt * 1e3, 3), "Gelem_s": round(n / dt / 1e9, 3), "GB_s": round(nbytes / dt / 1e9, 1)}
+
+    out = {"sample": f"2^{log_n} u32", "threads": t, "kind": "port"}
+    with ThreadPoolExecutor(max_workers=t) as ex:
+        for s in (1, 50, 99):
+            p = oracle.pred(1, 0, 100, s)
+            dt1, c1 = best_of(lambda: len(oracle.copy_if(x, 4, p)))
+
+            def par_copy_if():
+                tmp = [np.empty(hi - lo, np.uint32) for lo, hi in bounds]
+                cnt = list(ex.map(lambda i: lib.ox_copy_if(oracle._p(x[bounds[i][0]:]), oracle._p(tmp[i]),
+                                                             bounds[i][1] - bounds[i][0], 4, ctypes.byref(p)),
+                                  range(t)))
+                off = np.concatenate([[0], np.cumsum(cnt)])
+                res = np.empty(int(off[-1]), np.uint32)
+                list(ex.map(lambda i: res.__setitem__(slice(int(off[i]), int(off[i + 1])), tmp[i][:cnt[i]]),
+                            range(t)))
+                return len(res)
+
+            dtt, ct = best_of(par_copy_if)
+            assert c1 == ct
+            nbytes = 4 * n + 4 * c1
+            out[f"copy_if_s{s}"] = {"selected": c1, "one_core": rates(dt1, nbytes), "all_threads": rates(dtt, nbytes)}
+        dt1, r1 = best_of(lambda: oracle.exclusive_scan_u32(xs))
+
+        def par_scan():
+            res = np.empty(n, np.uint32)
+            list(ex.map(lambda i: lib.ox_exclusive_scan_u32(oracle._p(xs[bounds[i][0]:]), oracle._p(res[bounds[i][0]:]),
+                                                            bounds[i][1] - bounds[i][0]), range(t)))
+            tot = [int(res[hi - 1]) + int(xs[hi - 1]) for lo, hi in bounds]
+            off = np.concatenate([[0], np.cumsum(tot)]).astype(np.uint64) & np.uint64(0xFFFFFFFF)
+            list(ex.map(lambda i: np.add(res[bounds[i][0]:bounds[i][1]], np.uint32(off[i]),
+                                         out=res[bounds[i][0]:bounds[i][1]]), range(t)))
+            return res
+
+        dtt, rt = best_of(par_scan)
+        assert np.array_equal(r1, rt)
+        out["exclusive_scan"] = {"one_core": rates(dt1, 8 * n), "all_threads": rates(dtt, 8 * n)}
+    return out
 
 
 def run_batched(args, stream, dev):

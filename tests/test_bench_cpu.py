@@ -32,3 +32,16 @@ def test_reference_arm_json_line():
     assert cb["kind"] == "port" and cb["value"] == d["value"] and cb["unit"] == d["unit"] and cb["cores"] >= 1
     assert cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_cpu_streaming_baseline_small():
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    d = bench.cpu_streaming(log_n=16, threads=4, reps=1)  # asserts chunked == serial results inside
+    assert d["threads"] == 4 and d["kind"] == "port"
+    for s, lo, hi in ((1, 0.005, 0.02), (50, 0.45, 0.55), (99, 0.97, 1.0)):
+        r = d[f"copy_if_s{s}"]
+        assert lo < r["selected"] / (1 << 16) < hi
+        assert r["one_core"]["ms"] > 0 and r["all_threads"]["GB_s"] > 0
+    assert d["exclusive_scan"]["one_core"]["Gelem_s"] > 0
