@@ -226,6 +226,45 @@ def _guarded(fn):
         return {"error": f"{type(e).__name__}: {e}"}
 
 
+def cpu_batched(w: dict, gpu_out=None, threads: int | None = None, reps: int = 2) -> dict:
+    """CPU baseline of one batched round: for every map, the oracle's serial map (the reference's CPU path
+    restated) is created empty at its size power, then insert all (no growth), query, erase, clean_tombstones
+    — the same round as the fused GPU launch, maps dealt round-robin to host threads (the oracle's calls release
+    the GIL). If gpu_out (the fused launch's query outputs, pre-filled with all ones) is given, the CPU query
+    outputs are compared with it element for element."""
+    import oracle
+    from concurrent.futures import ThreadPoolExecutor
+    t = threads or host_threads()
+    io, qo, eo = (w[k].astype(np.int64) for k in ("ins_offsets", "query_offsets", "erase_offsets"))
+    sp = w["size_powers"]
+    keys, vals, qs, er = (np.ascontiguousarray(w[k]).view(np.uint32) for k in ("keys", "vals", "queries", "erase"))
+    out = np.full(len(qs), 0xFFFFFFFF, np.uint32)
+
+    def work(tid):
+        for i in range(tid, len(sp), t):
+            m = oracle.OracleMap(int(sp[i]), 4)
+            m.insert(keys[io[i]:io[i + 1]], vals[io[i]:io[i + 1]], 0.0)
+            m.retrieve(qs[qo[i]:qo[i + 1]], out[qo[i]:qo[i + 1]])
+            m.erase(er[eo[i]:eo[i + 1]])
+            m.clean_tombstones()
+            del m
+
+    best = None
+    with ThreadPoolExecutor(max_workers=t) as ex:
+        for _ in range(reps):
+            out.fill(0xFFFFFFFF)
+            t0 = time.perf_counter()
+            list(ex.map(work, range(t)))
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+    n_ops = len(keys) + len(qs) + len(er)
+    r = {"ms": round(best * 1e3, 1), "Mops_s": round(n_ops / best / 1e6, 1), "threads": t, "kind": "port",
+         "sample": "the whole round (every map), one serial map per map, maps dealt round-robin to host threads"}
+    if gpu_out is not None:
+        r["query_outputs_equal_gpu"] = bool(np.array_equal(out, np.asarray(gpu_out).view(np.uint32)))
+    return r
+
+
 def cpu_streaming(log_n: int = 24, threads: int | None = None, reps: int = 3) -> dict:
     """CPU baseline of the streaming primitives on a bounded sample of 2^log_n u32 (uniform; scan input in
     [0, 16)): the oracle's serial copy_if with (x % 100) < s, s = 1/50/99, and its serial exclusive scan, on one
@@ -360,7 +399,8 @@ def run_batched(args, stream, dev):
             "fused_Mops_s": round(n_ops / fused_ms / 1e3, 1), "plain_Mops_s": round(n_ops / plain_ms / 1e3, 1),
             "autotuned": {"group_width": tune["best"][0], "block": tune["best"][1], "tile_keys": tune["best"][2]},
             "bit_exact_vs_per_map": same_q and fills_equal and err == 0, "generate_s": round(gen_s, 1),
-            "timing": "CUDA events around clear + run, median; fused replays a captured CUDA graph"}
+            "timing": "CUDA events around clear + run, median; fused replays a captured CUDA graph",
+            "cpu_baseline": _guarded(lambda: cpu_batched(w, outs[0].cpu().numpy()))}
 
 
 def run_serving(args, dev):
@@ -800,7 +840,9 @@ def run_ours(args):
                     "note": "ceilings measured in this run by hx_diag_random_access over 1 GiB; frac = keys/s of the "
                             "dominant kernel over the ceiling of its one unavoidable random op per key (CAS for "
                             "insert, 32-byte read for query); DRAM transactions, not bytes, bound these kernels"},
-                "kernel": "k_insert_t1 (insert)" if dominant == "insert" else "k_find_t1 (query)",
+                "kernel": (("k_insert_t1 (insert)" if args.group in (0, 1) else "k_insert (insert)")
+                           if dominant == "insert" else
+                           ("k_find_t1 (query)" if args.group == 1 else "k_retrieve (query)")),
                 "algorithmic_bytes_per_launch": (INSERT_BYTES_PER_KEY if dominant == "insert"
                                                  else QUERY_BYTES_PER_KEY)[width] * n,
                 "per_op": {"insert": {"ms": round(t_ins * 1e3, 3), "Mkeys_s": round(n / t_ins / 1e6, 1),

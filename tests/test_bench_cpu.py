@@ -45,3 +45,23 @@ def test_cpu_streaming_baseline_small():
         assert lo < r["selected"] / (1 << 16) < hi
         assert r["one_core"]["ms"] > 0 and r["all_threads"]["GB_s"] > 0
     assert d["exclusive_scan"]["one_core"]["Gelem_s"] > 0
+
+
+def test_cpu_batched_baseline_against_a_dict_model():
+    sys.path.insert(0, str(ROOT))
+    import numpy as np
+    import bench
+    from hashinator_gb300 import workloads
+
+    w = workloads.batched_workload(48, 7)
+    io, qo = w["ins_offsets"].astype(np.int64), w["query_offsets"].astype(np.int64)
+    expect = np.full(len(w["queries"]), 0xFFFFFFFF, np.uint32)  # misses keep the pre-fill
+    for i in range(48):
+        d = dict(zip(w["keys"][io[i]:io[i + 1]].tolist(), w["vals"][io[i]:io[i + 1]].tolist()))
+        q = w["queries"][qo[i]:qo[i + 1]].tolist()
+        expect[qo[i]:qo[i + 1]] = [d.get(k, 0xFFFFFFFF) for k in q]
+    r = bench.cpu_batched(w, expect.view(np.int32), threads=4, reps=1)
+    assert r["query_outputs_equal_gpu"] is True and r["Mops_s"] > 0
+    bad = expect.copy()
+    bad[len(bad) // 2] ^= 1
+    assert bench.cpu_batched(w, bad, threads=2, reps=1)["query_outputs_equal_gpu"] is False
