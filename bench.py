@@ -830,7 +830,10 @@ def run_ours(args):
     q_gbs = QUERY_BYTES_PER_KEY[width] * n / t_q / 1e9
     dominant = "insert" if t_ins >= t_q else "query"
     achieved = ins_gbs if dominant == "insert" else q_gbs
-    traffic = traffic_from_profiles(f"{dominant}_u32_lf050")
+    # measured traffic (2^26 keys) exists for the thread-per-key insert and query kernels
+    tag = ("insert_u32_lf050" if args.group in (0, 1) else None) if dominant == "insert" else \
+        ("query_t1_u32_lf050" if args.group == 1 else None)
+    traffic = traffic_from_profiles(tag) if tag and args.log_keys == 26 else None
     dom_keys_s = n / (t_ins if dominant == "insert" else t_q)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
