@@ -296,23 +296,38 @@ class Hashmap {
   static_assert(std::is_same<KEY_TYPE, VAL_TYPE>::value &&
                     (std::is_same<KEY_TYPE, uint32_t>::value || std::is_same<KEY_TYPE, uint64_t>::value),
                 "libhx serves hash_pair<uint32_t,uint32_t> and hash_pair<uint64_t,uint64_t>");
-  static_assert(EMPTYBUCKET == std::numeric_limits<KEY_TYPE>::max() && TOMBSTONE == EMPTYBUCKET - 1,
-                "libhx uses the reference's default sentinels");
+  // libhx's tables use the reference's default sentinels (EMPTY = all ones,
+  // TOMBSTONE = EMPTY - 1). Other sentinels may be named, and
+  // get_emptybucket() / get_tombstone() report them (the reference's
+  // EMPTY_TOMBSTONE_values test), but every operation on the table goes
+  // through map() or view(), whose static_assert rejects them at compile time.
+  static constexpr bool kDefaultSentinels =
+      EMPTYBUCKET == std::numeric_limits<KEY_TYPE>::max() && TOMBSTONE == EMPTYBUCKET - 1;
   using pair_t = hash_pair<KEY_TYPE, VAL_TYPE>;
   using view_t = hx_device::MapView<KEY_TYPE, VAL_TYPE>;
   hx_map* m_ = nullptr;
   hx_device_view dv_{};      // what the device copy works on (refreshed by upload())
   Hashmap* d_self_ = nullptr;  // the device copy that upload() returns
 
-  __host__ __device__ view_t view() const { return view_t::from(dv_); }
-  __device__ pair_t* dbuckets() const { return static_cast<pair_t*>(dv_.buckets); }
+  hx_map* map() const {
+    static_assert(kDefaultSentinels, "libhx operates only on tables with the default sentinels");
+    return m_;
+  }
+  __host__ __device__ view_t view() const {
+    static_assert(kDefaultSentinels, "libhx operates only on tables with the default sentinels");
+    return view_t::from(dv_);
+  }
+  __device__ pair_t* dbuckets() const {
+    static_assert(kDefaultSentinels, "libhx operates only on tables with the default sentinels");
+    return static_cast<pair_t*>(dv_.buckets);
+  }
   __device__ size_t dsize() const { return (size_t)1 << dv_.size_power; }
   __device__ static bool valid(KEY_TYPE k) { return k != EMPTYBUCKET && k != TOMBSTONE; }
 
   void sync(cudaStream_t s) const { hxcompat::check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize"); }
   hx_info info(cudaStream_t s = 0) const {
     hx_info i;
-    hxcompat::check(hx_get_info(m_, &i, s), "hx_get_info");
+    hxcompat::check(hx_get_info(map(), &i, s), "hx_get_info");
     return i;
   }
 
@@ -332,60 +347,60 @@ class Hashmap {
   // ---- accelerated API (hashinator.h:1262-1409) ----
   template <bool prefetches = true>
   void insert(KEY_TYPE* keys, VAL_TYPE* vals, size_t len, float targetLF = 0.5, cudaStream_t s = 0) {
-    hxcompat::check(hx_insert(m_, keys, vals, len, targetLF, s), "hx_insert");
+    hxcompat::check(hx_insert(map(), keys, vals, len, targetLF, s), "hx_insert");
     sync(s);
   }
   template <bool prefetches = true>
   void insert(pair_t* src, size_t len, float targetLF = 0.5, cudaStream_t s = 0) {
-    hxcompat::check(hx_insert_pairs(m_, src, len, targetLF, s), "hx_insert_pairs");
+    hxcompat::check(hx_insert_pairs(map(), src, len, targetLF, s), "hx_insert_pairs");
     sync(s);
   }
   template <bool prefetches = true>
   void retrieve(KEY_TYPE* keys, VAL_TYPE* vals, size_t len, cudaStream_t s = 0) {
-    hxcompat::check(hx_retrieve(m_, keys, vals, len, s), "hx_retrieve");
+    hxcompat::check(hx_retrieve(map(), keys, vals, len, s), "hx_retrieve");
     sync(s);
   }
   template <bool prefetches = true>
   void retrieve(pair_t* src, size_t len, cudaStream_t s = 0) {
-    hxcompat::check(hx_retrieve_pairs(m_, src, len, s), "hx_retrieve_pairs");
+    hxcompat::check(hx_retrieve_pairs(map(), src, len, s), "hx_retrieve_pairs");
     sync(s);
   }
   template <bool prefetches = true>
   void erase(KEY_TYPE* keys, size_t len, cudaStream_t s = 0) {
-    hxcompat::check(hx_erase(m_, keys, len, s), "hx_erase");
+    hxcompat::check(hx_erase(map(), keys, len, s), "hx_erase");
     sync(s);
   }
   template <bool prefetches = true>
   void clean_tombstones(cudaStream_t s = 0) {
-    hxcompat::check(hx_clean_tombstones(m_, s), "hx_clean_tombstones");
+    hxcompat::check(hx_clean_tombstones(map(), s), "hx_clean_tombstones");
     sync(s);
   }
   template <bool prefetches = true>
   void device_rehash(int newSizePower, cudaStream_t s = 0) {
-    hxcompat::check(hx_resize(m_, newSizePower, s), "hx_resize");
+    hxcompat::check(hx_resize(map(), newSizePower, s), "hx_resize");
     sync(s);
   }
   void resize(int newSizePower, targets = targets::device, cudaStream_t s = 0) { device_rehash(newSizePower, s); }
   template <bool prefetches = true>
   void clear(targets = targets::device, cudaStream_t s = 0, size_t = 0) {
-    hxcompat::check(hx_clear(m_, s), "hx_clear");
+    hxcompat::check(hx_clear(map(), s), "hx_clear");
     sync(s);
   }
 
   /* insertIndex(keys, len, targetLF, s) (hashinator.h:1339): keys[i] -> i. */
   template <bool prefetches = true>
   void insertIndex(KEY_TYPE* keys, size_t len, float targetLF = 0.5, cudaStream_t s = 0) {
-    hxcompat::check(hx_insert_index(m_, keys, len, targetLF, s), "hx_insert_index");
+    hxcompat::check(hx_insert_index(map(), keys, len, targetLF, s), "hx_insert_index");
     sync(s);
   }
   /* resize_to_lf(targetLF, targets, s) (hashinator.h:530). */
   void resize_to_lf(float targetLF = 0.5, targets = targets::device, cudaStream_t s = 0) {
-    hxcompat::check(hx_resize_to_lf(m_, targetLF, s), "hx_resize_to_lf");
+    hxcompat::check(hx_resize_to_lf(map(), targetLF, s), "hx_resize_to_lf");
   }
   /* performCleanupTasks(s) (hashinator.h:643). */
   template <bool prefetches = true>
   void performCleanupTasks(cudaStream_t s = 0) {
-    hxcompat::check(hx_perform_cleanup_tasks(m_, s), "hx_perform_cleanup_tasks");
+    hxcompat::check(hx_perform_cleanup_tasks(map(), s), "hx_perform_cleanup_tasks");
   }
 
   /* extractKeysByPattern(SplitVector<KEY>&, Rule, s) (hashinator.h:1199):
@@ -394,12 +409,12 @@ class Hashmap {
   size_t extractKeysByPattern(split::SplitVector<KEY_TYPE>& elements, Rule rule, cudaStream_t s = 0) {
     void* b = nullptr;
     uint64_t nb = 0;
-    hxcompat::check(hx_bucket_data(m_, &b, &nb), "hx_bucket_data");
+    hxcompat::check(hx_bucket_data(map(), &b, &nb), "hx_bucket_data");
     elements.resize(nb);
     size_t c;
     if constexpr (std::is_same<Rule, hx_pred>::value) {
       uint64_t h = 0;
-      const hx_status st = hx_extract_keys(m_, &rule, elements.data(), nb, nullptr, &h, s);
+      const hx_status st = hx_extract_keys(map(), &rule, elements.data(), nb, nullptr, &h, s);
       if (st != HX_OK && st != HX_ERR_CAPACITY) hxcompat::check(st, "hx_extract_keys");
       c = (size_t)h;
     } else {
@@ -432,10 +447,10 @@ class Hashmap {
   size_t extractPattern(pair_t* elements, Rule rule, cudaStream_t s = 0) {
     void* b = nullptr;
     uint64_t nb = 0;
-    hxcompat::check(hx_bucket_data(m_, &b, &nb), "hx_bucket_data");
+    hxcompat::check(hx_bucket_data(map(), &b, &nb), "hx_bucket_data");
     if constexpr (std::is_same<Rule, hx_pred>::value) {
       uint64_t c = 0;
-      const hx_status st = hx_extract_pattern(m_, &rule, elements, nb, nullptr, &c, s);
+      const hx_status st = hx_extract_pattern(map(), &rule, elements, nb, nullptr, &c, s);
       if (st != HX_OK && st != HX_ERR_CAPACITY) hxcompat::check(st, "hx_extract_pattern");
       return (size_t)c;
     } else {
@@ -449,7 +464,7 @@ class Hashmap {
   size_t extractPattern(split::SplitVector<pair_t>& elements, Rule rule, cudaStream_t s = 0) {
     void* b = nullptr;
     uint64_t nb = 0;
-    hxcompat::check(hx_bucket_data(m_, &b, &nb), "hx_bucket_data");
+    hxcompat::check(hx_bucket_data(map(), &b, &nb), "hx_bucket_data");
     elements.resize(nb);
     const size_t c = extractPattern(elements.data(), rule, s);
     elements.erase(elements.data() + c, elements.end());
@@ -459,7 +474,7 @@ class Hashmap {
   // ---- metadata (hashinator.h:434-457, 611, 228) ----
   status peek_status() {
     int32_t v = 0;
-    hxcompat::check(hx_peek_status(m_, &v, nullptr), "hx_peek_status");
+    hxcompat::check(hx_peek_status(map(), &v, nullptr), "hx_peek_status");
     return static_cast<status>(v);
   }
   int getSizePower() const { return info().size_power; }
@@ -480,19 +495,19 @@ class Hashmap {
   template <bool warn = true>
   pair_t* expose_bucketdata() {
     void* b = nullptr;
-    hxcompat::check(hx_bucket_data(m_, &b, nullptr), "hx_bucket_data");
+    hxcompat::check(hx_bucket_data(map(), &b, nullptr), "hx_bucket_data");
     return static_cast<pair_t*>(b);
   }
   void optimizeGPU(cudaStream_t = 0) {}
   void optimizeCPU(cudaStream_t = 0) {}
-  hx_map* handle() { return m_; }
+  hx_map* handle() { return map(); }
 
   // ---- device API (hashinator.h:853-1126, 1417-1769) ----
   /* upload(s) (hashinator.h:1417): a device copy of this map for kernels;
    * call it again after any host call that may reallocate the table. */
   template <bool prefetches = true>
   Hashmap* upload(cudaStream_t s = 0) {
-    hxcompat::check(hx_map_device_view(m_, &dv_), "hx_map_device_view");
+    hxcompat::check(hx_map_device_view(map(), &dv_), "hx_map_device_view");
     if (!d_self_) hxcompat::check_cuda(cudaMalloc(&d_self_, sizeof(Hashmap)), "cudaMalloc");
     hxcompat::check_cuda(cudaMemcpyAsync(d_self_, this, sizeof(Hashmap), cudaMemcpyHostToDevice, s),
                          "cudaMemcpyAsync");

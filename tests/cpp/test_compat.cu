@@ -3,6 +3,8 @@
 //   test_hashmap_4          unit_tests/hashmap_unit_test/main.cu:726-785
 //   Test_Duplicate_Insertion                          main.cu:1064-1085
 //   Test_ErrorCodes_ExtractKeysByPattern-style rule   main.cu:975-1019
+//   Test_Copy_Metadata                                main.cu:1022-1037
+//   EMPTY_TOMBSTONE_values (custom sentinels named)   main.cu:1087-1094
 //   Compaction_Tests_Linear / _Power_of_2   unit_tests/stream_compaction/unit.cu:133-153
 //   prefix scan of input[i] = i             unit_tests/stream_compaction/race.cu:100-113
 // A tiny harness stands in for gtest (not installed). Exit code 0 = all pass.
@@ -127,6 +129,28 @@ static void test_extract_rules() {
   EXPECT_TRUE(even_valid == N / 2 && ce >= N / 2);
 }
 
+static void test_copy_metadata() {  // hashmap_unit_test/main.cu:1022-1037
+  vector src(size_t(1) << 18);
+  create_input(src);
+  hashmap hmap;
+  hmap.insert(src.data(), src.size());
+  EXPECT_TRUE(recover(hmap, src, false));
+  EXPECT_TRUE(hmap.peek_status() == status::success);
+  Info info;
+  hmap.copyMetadata(&info);
+  EXPECT_TRUE((size_t(1) << info.sizePower) == hmap.bucket_count());
+  EXPECT_TRUE(info.tombstoneCounter == hmap.tombstone_count());
+  EXPECT_TRUE(info.fill == src.size());
+}
+
+static void test_custom_sentinels() {  // hashmap_unit_test/main.cu:1087-1094
+  Hashmap<key_type, val_type, 42, 42> hmap;
+  const auto tombstone = hmap.get_tombstone();
+  const auto emptybucket = hmap.get_emptybucket();
+  EXPECT_TRUE(tombstone == emptybucket && tombstone == 42);
+  static_assert(tombstone == emptybucket, "the sentinels are compile-time constants");
+}
+
 struct test_t {
   uint32_t num, flag;
 };
@@ -166,6 +190,8 @@ int main() {
   for (int p = 10; p <= 16; p += 3) test_hashmap_4(p);
   test_duplicate_insertion();
   test_extract_rules();
+  test_copy_metadata();
+  test_custom_sentinels();
   for (size_t s = 32; s < 3000; s += 37) EXPECT_TRUE(compaction_flags(s));
   for (int p = 5; p < 20; p += 2) EXPECT_TRUE(compaction_flags(size_t(1) << p));
   for (int p = 2; p < 18; ++p) EXPECT_TRUE(scan_iota(size_t(1) << p));
