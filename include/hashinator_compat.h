@@ -7,7 +7,8 @@
  *   Hashinator::hash_pair<K,V>    hashinator/hash_pair.h:30-75
  *   Hashinator::Info / status     hashinator/defaults.h:44-54, common.h:85
  *   split::SplitVector<T>         splitvector/splitvec.h:83 (managed memory, minimal surface)
- *   split::tools::copy_if         splitvector/split_tools.h:1129-1223
+ *   split::tools::copy_if, copy_keys_if, splitStackArena,
+ *   estimateMemoryForCompaction   splitvector/split_tools.h:491-535, 1065-1223
  *   split::tools::split_prefix_scan  split_tools.h:363-418
  *   device API (upload/download, device_find/insert/erase, iterators,
  *   warpInsert/warpFind/warpErase)   hashinator.h:853-1126, 1417-1769
@@ -274,6 +275,91 @@ void copy_if(SplitVector<T>& input, SplitVector<T>& output, Rule rule, cudaStrea
 template <typename T, typename Rule>
 size_t copy_if(T* input, T* output, size_t size, Rule rule, void* /*stack*/, size_t /*max_size*/, cudaStream_t s = 0) {
   return detail::copy_if_functor(input, output, size, size, rule, detail::Identity{}, s);
+}
+
+/* splitStackArena (split_tools.h:491-535): a bump allocator over one device
+ * buffer, either allocated stream-ordered (and freed with the arena) or
+ * borrowed from the caller. libhx's compaction takes its scratch from the
+ * device's stream-ordered pool itself, so the copy_if / copy_keys_if
+ * overloads below accept an arena or a (stack, max_size) buffer for source
+ * compatibility and leave it untouched. */
+class splitStackArena {
+  void* base_ = nullptr;
+  size_t cap_ = 0, used_ = 0;
+  cudaStream_t s_ = 0;
+  bool owned_ = false;
+
+ public:
+  explicit splitStackArena(size_t bytes, cudaStream_t s) : cap_(bytes), s_(s), owned_(true) {
+    hxcompat::check_cuda(cudaMallocAsync(&base_, bytes, s), "cudaMallocAsync");
+  }
+  explicit splitStackArena(void* ptr, size_t bytes) : base_(ptr), cap_(bytes) {}
+  splitStackArena() = delete;
+  splitStackArena(const splitStackArena&) = delete;
+  splitStackArena(splitStackArena&&) = delete;
+  ~splitStackArena() {
+    if (owned_ && base_) cudaFreeAsync(base_, s_);
+  }
+  void* allocate(size_t bytes) {
+    if (used_ + bytes > cap_) {
+      std::fprintf(stderr, "splitStackArena: %zu bytes requested, %zu free\n", bytes, cap_ - used_);
+      std::abort();
+    }
+    void* p = static_cast<char*>(base_) + used_;
+    used_ += bytes;
+    return p;
+  }
+  void deallocate(size_t bytes) { used_ -= bytes; }
+  void reset() { used_ = 0; }
+  const size_t& fill() const { return used_; }
+  const size_t& capacity() const { return cap_; }
+  size_t free_space() const { return cap_ - used_; }
+};
+
+/* estimateMemoryForCompaction (split_tools.h:1065-1090): the device scratch
+ * that libhx's compaction of inputSize elements uses (hx_scratch_bytes). */
+template <int BLOCKSIZE = 1024>
+[[nodiscard]] size_t estimateMemoryForCompaction(const size_t inputSize) noexcept {
+  uint64_t b = 0;
+  return hx_scratch_bytes(HX_SCRATCH_COPY_IF, inputSize, &b) == HX_OK ? (size_t)b : 0;
+}
+template <typename T, int BLOCKSIZE = 1024>
+[[nodiscard]] size_t estimateMemoryForCompaction(const SplitVector<T>& input) noexcept {
+  return estimateMemoryForCompaction<BLOCKSIZE>(input.size());
+}
+
+/* copy_if(in, out, rule, splitStackArena&&, stream) (split_tools.h:1162)
+ * and copy_if(in, out, rule, stack, max_size, stream) (:1194). */
+template <typename T, typename Rule>
+void copy_if(SplitVector<T>& input, SplitVector<T>& output, Rule rule, splitStackArena&& /*mPool*/,
+             cudaStream_t s = 0) {
+  copy_if(input, output, rule, s);
+}
+template <typename T, typename Rule>
+void copy_if(SplitVector<T>& input, SplitVector<T>& output, Rule rule, void* /*stack*/, size_t /*max_size*/,
+             cudaStream_t s = 0) {
+  copy_if(input, output, rule, s);
+}
+
+/* copy_keys_if(in, out, rule, stream) (split_tools.h:1095) and its arena
+ * (:1147) and stack (:1177) forms: the keys of the selected hash_pairs, in
+ * order; out must hold the result and is resized to the count. The rule is
+ * a functor over the pair. */
+template <typename T, typename U, typename Rule>
+void copy_keys_if(SplitVector<T>& input, SplitVector<U>& output, Rule rule, cudaStream_t s = 0) {
+  const size_t c = detail::copy_if_functor(input.data(), output.data(), input.size(), output.size(), rule,
+                                           detail::KeyOf{}, s);
+  output.erase(output.data() + (c < output.size() ? c : output.size()), output.end());
+}
+template <typename T, typename U, typename Rule>
+void copy_keys_if(SplitVector<T>& input, SplitVector<U>& output, Rule rule, splitStackArena&& /*mPool*/,
+                  cudaStream_t s = 0) {
+  copy_keys_if(input, output, rule, s);
+}
+template <typename T, typename U, typename Rule>
+void copy_keys_if(SplitVector<T>& input, SplitVector<U>& output, Rule rule, void* /*stack*/, size_t /*max_size*/,
+                  cudaStream_t s = 0) {
+  copy_keys_if(input, output, rule, s);
 }
 
 /* split_prefix_scan(in, out, stream) (split_tools.h:363): exclusive sum of

@@ -5,6 +5,7 @@
 //   Test_ErrorCodes_ExtractKeysByPattern-style rule   main.cu:975-1019
 //   Test_Copy_Metadata                                main.cu:1022-1037
 //   EMPTY_TOMBSTONE_values (custom sentinels named)   main.cu:1087-1094
+//   arena / stack copy_if and copy_keys_if  unit_tests/stream_compaction/preallocated.cu
 //   Compaction_Tests_Linear / _Power_of_2   unit_tests/stream_compaction/unit.cu:133-153
 //   prefix scan of input[i] = i             unit_tests/stream_compaction/race.cu:100-113
 // A tiny harness stands in for gtest (not installed). Exit code 0 = all pass.
@@ -151,6 +152,46 @@ static void test_custom_sentinels() {  // hashmap_unit_test/main.cu:1087-1094
   static_assert(tombstone == emptybucket, "the sentinels are compile-time constants");
 }
 
+// copy_if with an owned arena and with a caller stack, copy_keys_if in its
+// three forms, and the arena's bump allocation (split_tools.h:491-535,
+// 1065-1223; the arena use of stream_compaction/preallocated.cu).
+static void test_arena_and_key_overloads() {
+  const size_t N = 5000;
+  vector src(N);
+  create_input(src);  // (i, i): the even values sit at even i
+  const size_t bytes = split::tools::estimateMemoryForCompaction(src);
+  EXPECT_TRUE(bytes >= 64 && bytes == split::tools::estimateMemoryForCompaction<1024>(N));
+  void* stack = nullptr;
+  cudaMalloc(&stack, bytes);
+  vector o1(N), o2(N);
+  split::tools::copy_if(src, o1, Predicate(), split::tools::splitStackArena(bytes, 0));
+  split::tools::copy_if(src, o2, Predicate(), stack, bytes);
+  EXPECT_TRUE(o1.size() == N / 2 && o2.size() == N / 2);
+  bool ok = true;
+  for (size_t i = 0; i < o1.size() && i < o2.size(); ++i)
+    ok = ok && o1[i].first == 2 * i && o1[i].second == 2 * i && o2[i] == o1[i];
+  EXPECT_TRUE(ok);
+  split::SplitVector<key_type> k1(N), k2(N), k3(N);
+  split::tools::copy_keys_if(src, k1, Predicate());
+  split::tools::copy_keys_if(src, k2, Predicate(), split::tools::splitStackArena(bytes, 0));
+  split::tools::copy_keys_if(src, k3, Predicate(), stack, bytes);
+  EXPECT_TRUE(k1.size() == N / 2 && k2.size() == N / 2 && k3.size() == N / 2);
+  ok = true;
+  for (size_t i = 0; i < k1.size() && i < k2.size() && i < k3.size(); ++i)
+    ok = ok && k1[i] == 2 * i && k2[i] == 2 * i && k3[i] == 2 * i;
+  EXPECT_TRUE(ok);
+  split::tools::splitStackArena a(stack, bytes);
+  char* p0 = static_cast<char*>(a.allocate(16));
+  char* p1 = static_cast<char*>(a.allocate(32));
+  EXPECT_TRUE(p0 == stack && p1 == p0 + 16 && a.fill() == 48 && a.free_space() == bytes - 48);
+  a.deallocate(32);
+  EXPECT_TRUE(a.fill() == 16);
+  a.reset();
+  EXPECT_TRUE(a.fill() == 0 && a.capacity() == bytes);
+  cudaDeviceSynchronize();
+  cudaFree(stack);
+}
+
 struct test_t {
   uint32_t num, flag;
 };
@@ -192,6 +233,7 @@ int main() {
   test_extract_rules();
   test_copy_metadata();
   test_custom_sentinels();
+  test_arena_and_key_overloads();
   for (size_t s = 32; s < 3000; s += 37) EXPECT_TRUE(compaction_flags(s));
   for (int p = 5; p < 20; p += 2) EXPECT_TRUE(compaction_flags(size_t(1) << p));
   for (int p = 2; p < 18; ++p) EXPECT_TRUE(scan_iota(size_t(1) << p));
