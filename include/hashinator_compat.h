@@ -29,6 +29,8 @@
 #include <cstdlib>
 #include <limits>
 #include <type_traits>
+#include <utility>
+#include <vector>
 
 #include "hx.h"
 #include "hx_device_api.cuh"
@@ -586,7 +588,73 @@ class Hashmap {
   }
   void optimizeGPU(cudaStream_t = 0) {}
   void optimizeCPU(cudaStream_t = 0) {}
+  // The table is device resident, so unified-memory advice and stream
+  // attachment (hashinator.h:1129, 1440) have nothing to act on.
+  void memAdvise(cudaMemoryAdvise, int, cudaStream_t = 0) {}
+  void streamAttach(cudaStream_t, uint32_t = cudaMemAttachSingle) {}
   hx_map* handle() { return map(); }
+
+  /* rehash(newSizePower) (hashinator.h:236): the same result as
+   * device_rehash — every valid pair in a table of 2^newSizePower buckets. */
+  void rehash(int newSizePower) { device_rehash(newSizePower); }
+  /* tombstone_ratio() (hashinator.h:614). */
+  float tombstone_ratio() const {
+    const hx_info i = info();
+    return i.tombstone_counter ? (float)i.tombstone_counter / (float)i.bucket_count : 0.0f;
+  }
+  /* swap(other) (hashinator.h:622): exchanges the two tables. */
+  void swap(Hashmap& other) noexcept {
+    std::swap(m_, other.m_);
+    std::swap(dv_, other.dv_);
+    std::swap(d_self_, other.d_self_);
+  }
+  /* stats() and dump_buckets() (hashinator.h:591-611): metadata, and every
+   * bucket with its distance from home, printed on the host. */
+  void stats() const {
+    const hx_info i = info();
+    std::printf("Hashmap: 2^%d buckets, fill %llu (load factor %.4f), tombstones %llu, probe bound %llu\n",
+                i.size_power, (unsigned long long)i.fill, (double)i.fill / (double)i.bucket_count,
+                (unsigned long long)i.tombstone_counter, (unsigned long long)i.current_max_bucket_overflow);
+  }
+  void dump_buckets() const {
+    stats();
+    void* b = nullptr;
+    uint64_t nb = 0;
+    hxcompat::check(hx_bucket_data(map(), &b, &nb), "hx_bucket_data");
+    std::vector<pair_t> h(nb);
+    hxcompat::check_cuda(cudaMemcpy(h.data(), b, nb * sizeof(pair_t), cudaMemcpyDeviceToHost), "cudaMemcpy");
+    const int sp = getSizePower();
+    for (uint64_t j = 0; j < nb; ++j) {
+      const KEY_TYPE k = h[j].first;
+      if (k == EMPTYBUCKET) {
+        std::printf(". ");
+      } else if (k == TOMBSTONE) {
+        std::printf("x ");
+      } else {
+        const uint64_t home = (uint64_t)hx_device::home(k, sp);
+        std::printf("(%llu,%llu,+%llu) ", (unsigned long long)k, (unsigned long long)h[j].second,
+                    (unsigned long long)((j - home) & (nb - 1)));
+      }
+    }
+    std::printf("\n");
+  }
+
+  /* The single-block "loop" extractions (hashinator.h:1187-1260) keep their
+   * count on the device in the reference; here they run the same selection
+   * as extractPattern / extractKeysByPattern and size `elements` on the
+   * host, so the elements are the same once the stream has finished. */
+  template <typename Rule>
+  void extractPatternLoop(split::SplitVector<pair_t>& elements, Rule rule, cudaStream_t s = 0) {
+    extractPattern(elements, rule, s);
+  }
+  void extractLoop(split::SplitVector<pair_t>& elements, cudaStream_t s = 0) {
+    extractPattern(elements, hx_pred{HX_PRED_VALID, HX_FIELD_KEY, 0, 0, 0, 0}, s);
+  }
+  template <typename Rule>
+  void extractKeysByPatternLoop(split::SplitVector<KEY_TYPE>& elements, Rule rule, cudaStream_t s = 0) {
+    extractKeysByPattern(elements, rule, s);
+  }
+  void extractAllKeysLoop(split::SplitVector<KEY_TYPE>& elements, cudaStream_t s = 0) { extractAllKeys(elements, s); }
 
   // ---- device API (hashinator.h:853-1126, 1417-1769) ----
   /* upload(s) (hashinator.h:1417): a device copy of this map for kernels;

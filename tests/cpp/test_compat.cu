@@ -6,6 +6,7 @@
 //   Test_Copy_Metadata                                main.cu:1022-1037
 //   EMPTY_TOMBSTONE_values (custom sentinels named)   main.cu:1087-1094
 //   arena / stack copy_if and copy_keys_if  unit_tests/stream_compaction/preallocated.cu
+//   swap, rehash, tombstone_ratio, loop extractions, stats  hashinator.h:236, 591-627, 1187-1260
 //   Compaction_Tests_Linear / _Power_of_2   unit_tests/stream_compaction/unit.cu:133-153
 //   prefix scan of input[i] = i             unit_tests/stream_compaction/race.cu:100-113
 // A tiny harness stands in for gtest (not installed). Exit code 0 = all pass.
@@ -192,6 +193,49 @@ static void test_arena_and_key_overloads() {
   cudaFree(stack);
 }
 
+// swap, rehash, tombstone_ratio, the "loop" extractions, the no-op memory
+// hints and the printing helpers (hashinator.h:236, 591-627, 1129,
+// 1187-1260, 1440).
+static void test_more_host_methods() {
+  const size_t N = 1000;
+  vector src(N);
+  create_input(src);
+  hashmap a(12), b(6);
+  a.insert(src.data(), N, 1.0f);
+  a.swap(b);
+  EXPECT_TRUE(a.size() == 0 && a.getSizePower() == 6 && b.size() == N && b.getSizePower() == 12);
+  b.rehash(13);
+  EXPECT_TRUE(b.size() == N && b.getSizePower() == 13 && recover(b, src, false));
+  split::SplitVector<key_type> evens;
+  for (size_t i = 0; i < N; i += 2) evens.push_back((key_type)i);
+  b.erase(evens.data(), evens.size());
+  EXPECT_TRUE(b.tombstone_count() == N / 2);
+  EXPECT_TRUE(b.tombstone_ratio() == (float)(N / 2) / (float)(1 << 13));
+  EXPECT_TRUE(a.tombstone_ratio() == 0.0f);
+  auto odd_valid = [] __host__ __device__(hash_pair<key_type, val_type> & e) -> bool {
+    return e.first != 0xFFFFFFFFu && e.first != 0xFFFFFFFEu && e.second % 2 == 1;
+  };
+  vector e1, e2;
+  split::SplitVector<key_type> k1, k2;
+  b.extractLoop(e1);
+  b.extractPatternLoop(e2, odd_valid);
+  b.extractAllKeysLoop(k1);
+  b.extractKeysByPatternLoop(k2, odd_valid);
+  EXPECT_TRUE(e1.size() == N / 2 && e2.size() == N / 2 && k1.size() == N / 2 && k2.size() == N / 2);
+  bool ok = true;
+  for (auto& e : e1) ok = ok && e.first % 2 == 1 && e.second == e.first;
+  for (size_t i = 0; i < e2.size() && i < e1.size(); ++i) ok = ok && e2[i] == e1[i];  // both in bucket order
+  for (size_t i = 0; i < k1.size() && i < e1.size(); ++i) ok = ok && k1[i] == e1[i].first && k2[i] == k1[i];
+  EXPECT_TRUE(ok);
+  b.memAdvise(cudaMemAdviseSetPreferredLocation, 0);
+  b.streamAttach(0);
+  b.stats();
+  hashmap tiny(4);
+  tiny.insert(src.data(), 3, 1.0f);
+  tiny.dump_buckets();
+  EXPECT_TRUE(tiny.size() == 3);
+}
+
 struct test_t {
   uint32_t num, flag;
 };
@@ -234,6 +278,7 @@ int main() {
   test_copy_metadata();
   test_custom_sentinels();
   test_arena_and_key_overloads();
+  test_more_host_methods();
   for (size_t s = 32; s < 3000; s += 37) EXPECT_TRUE(compaction_flags(s));
   for (int p = 5; p < 20; p += 2) EXPECT_TRUE(compaction_flags(size_t(1) << p));
   for (int p = 2; p < 18; ++p) EXPECT_TRUE(scan_iota(size_t(1) << p));
