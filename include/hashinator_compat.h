@@ -364,6 +364,22 @@ void copy_keys_if(SplitVector<T>& input, SplitVector<U>& output, Rule rule, void
   copy_keys_if(input, output, rule, s);
 }
 
+/* copy_if_loop / copy_if_keys_loop (split_tools.h:995-1020): the reference's
+ * single-block compactions, which write into the output's capacity and set
+ * its size on the device. Here they run copy_if / copy_keys_if into the
+ * output's capacity and set its size on the host; the elements and the size
+ * are the same once the stream has finished. */
+template <typename T, typename Rule>
+void copy_if_loop(SplitVector<T>& input, SplitVector<T>& output, Rule rule, cudaStream_t s = 0) {
+  output.resize(output.capacity());
+  copy_if(input, output, rule, s);
+}
+template <typename T, typename U, typename Rule>
+void copy_if_keys_loop(SplitVector<T>& input, SplitVector<U>& output, Rule rule, cudaStream_t s = 0) {
+  output.resize(output.capacity());
+  copy_keys_if(input, output, rule, s);
+}
+
 /* split_prefix_scan(in, out, stream) (split_tools.h:363): exclusive sum of
  * uint32_t, any length (the reference asserts a power of two). */
 inline void split_prefix_scan(SplitVector<uint32_t>& input, SplitVector<uint32_t>& output, cudaStream_t s = 0) {

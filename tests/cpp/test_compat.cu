@@ -181,6 +181,16 @@ static void test_arena_and_key_overloads() {
   for (size_t i = 0; i < k1.size() && i < k2.size() && i < k3.size(); ++i)
     ok = ok && k1[i] == 2 * i && k2[i] == 2 * i && k3[i] == 2 * i;
   EXPECT_TRUE(ok);
+  vector o3;
+  split::SplitVector<key_type> k4;
+  o3.reserve(N);  // the loop forms fill the output's capacity
+  k4.reserve(N);
+  split::tools::copy_if_loop(src, o3, Predicate());
+  split::tools::copy_if_keys_loop(src, k4, Predicate());
+  EXPECT_TRUE(o3.size() == N / 2 && k4.size() == N / 2);
+  ok = true;
+  for (size_t i = 0; i < o3.size() && i < k4.size() && i < o1.size(); ++i) ok = ok && o3[i] == o1[i] && k4[i] == 2 * i;
+  EXPECT_TRUE(ok);
   split::tools::splitStackArena a(stack, bytes);
   char* p0 = static_cast<char*>(a.allocate(16));
   char* p1 = static_cast<char*>(a.allocate(32));
