@@ -3,10 +3,6 @@
 //   test_hashmap_4          unit_tests/hashmap_unit_test/main.cu:726-785
 //   Test_Duplicate_Insertion                          main.cu:1064-1085
 //   Test_ErrorCodes_ExtractKeysByPattern-style rule   main.cu:975-1019
-//   Test_Copy_Metadata                                main.cu:1022-1037
-//   EMPTY_TOMBSTONE_values (custom sentinels named)   main.cu:1087-1094
-//   arena / stack copy_if and copy_keys_if  unit_tests/stream_compaction/preallocated.cu
-//   swap, rehash, tombstone_ratio, loop extractions, stats  hashinator.h:236, 591-627, 1187-1260
 //   Compaction_Tests_Linear / _Power_of_2   unit_tests/stream_compaction/unit.cu:133-153
 //   prefix scan of input[i] = i             unit_tests/stream_compaction/race.cu:100-113
 // A tiny harness stands in for gtest (not installed). Exit code 0 = all pass.
@@ -131,121 +127,6 @@ static void test_extract_rules() {
   EXPECT_TRUE(even_valid == N / 2 && ce >= N / 2);
 }
 
-static void test_copy_metadata() {  // hashmap_unit_test/main.cu:1022-1037
-  vector src(size_t(1) << 18);
-  create_input(src);
-  hashmap hmap;
-  hmap.insert(src.data(), src.size());
-  EXPECT_TRUE(recover(hmap, src, false));
-  EXPECT_TRUE(hmap.peek_status() == status::success);
-  Info info;
-  hmap.copyMetadata(&info);
-  EXPECT_TRUE((size_t(1) << info.sizePower) == hmap.bucket_count());
-  EXPECT_TRUE(info.tombstoneCounter == hmap.tombstone_count());
-  EXPECT_TRUE(info.fill == src.size());
-}
-
-static void test_custom_sentinels() {  // hashmap_unit_test/main.cu:1087-1094
-  Hashmap<key_type, val_type, 42, 42> hmap;
-  const auto tombstone = hmap.get_tombstone();
-  const auto emptybucket = hmap.get_emptybucket();
-  EXPECT_TRUE(tombstone == emptybucket && tombstone == 42);
-  static_assert(tombstone == emptybucket, "the sentinels are compile-time constants");
-}
-
-// copy_if with an owned arena and with a caller stack, copy_keys_if in its
-// three forms, and the arena's bump allocation (split_tools.h:491-535,
-// 1065-1223; the arena use of stream_compaction/preallocated.cu).
-static void test_arena_and_key_overloads() {
-  const size_t N = 5000;
-  vector src(N);
-  create_input(src);  // (i, i): the even values sit at even i
-  const size_t bytes = split::tools::estimateMemoryForCompaction(src);
-  EXPECT_TRUE(bytes >= 64 && bytes == split::tools::estimateMemoryForCompaction<1024>(N));
-  void* stack = nullptr;
-  cudaMalloc(&stack, bytes);
-  vector o1(N), o2(N);
-  split::tools::copy_if(src, o1, Predicate(), split::tools::splitStackArena(bytes, 0));
-  split::tools::copy_if(src, o2, Predicate(), stack, bytes);
-  EXPECT_TRUE(o1.size() == N / 2 && o2.size() == N / 2);
-  bool ok = true;
-  for (size_t i = 0; i < o1.size() && i < o2.size(); ++i)
-    ok = ok && o1[i].first == 2 * i && o1[i].second == 2 * i && o2[i] == o1[i];
-  EXPECT_TRUE(ok);
-  split::SplitVector<key_type> k1(N), k2(N), k3(N);
-  split::tools::copy_keys_if(src, k1, Predicate());
-  split::tools::copy_keys_if(src, k2, Predicate(), split::tools::splitStackArena(bytes, 0));
-  split::tools::copy_keys_if(src, k3, Predicate(), stack, bytes);
-  EXPECT_TRUE(k1.size() == N / 2 && k2.size() == N / 2 && k3.size() == N / 2);
-  ok = true;
-  for (size_t i = 0; i < k1.size() && i < k2.size() && i < k3.size(); ++i)
-    ok = ok && k1[i] == 2 * i && k2[i] == 2 * i && k3[i] == 2 * i;
-  EXPECT_TRUE(ok);
-  vector o3;
-  split::SplitVector<key_type> k4;
-  o3.reserve(N);  // the loop forms fill the output's capacity
-  k4.reserve(N);
-  split::tools::copy_if_loop(src, o3, Predicate());
-  split::tools::copy_if_keys_loop(src, k4, Predicate());
-  EXPECT_TRUE(o3.size() == N / 2 && k4.size() == N / 2);
-  ok = true;
-  for (size_t i = 0; i < o3.size() && i < k4.size() && i < o1.size(); ++i) ok = ok && o3[i] == o1[i] && k4[i] == 2 * i;
-  EXPECT_TRUE(ok);
-  split::tools::splitStackArena a(stack, bytes);
-  char* p0 = static_cast<char*>(a.allocate(16));
-  char* p1 = static_cast<char*>(a.allocate(32));
-  EXPECT_TRUE(p0 == stack && p1 == p0 + 16 && a.fill() == 48 && a.free_space() == bytes - 48);
-  a.deallocate(32);
-  EXPECT_TRUE(a.fill() == 16);
-  a.reset();
-  EXPECT_TRUE(a.fill() == 0 && a.capacity() == bytes);
-  cudaDeviceSynchronize();
-  cudaFree(stack);
-}
-
-// swap, rehash, tombstone_ratio, the "loop" extractions, the no-op memory
-// hints and the printing helpers (hashinator.h:236, 591-627, 1129,
-// 1187-1260, 1440).
-static void test_more_host_methods() {
-  const size_t N = 1000;
-  vector src(N);
-  create_input(src);
-  hashmap a(12), b(6);
-  a.insert(src.data(), N, 1.0f);
-  a.swap(b);
-  EXPECT_TRUE(a.size() == 0 && a.getSizePower() == 6 && b.size() == N && b.getSizePower() == 12);
-  b.rehash(13);
-  EXPECT_TRUE(b.size() == N && b.getSizePower() == 13 && recover(b, src, false));
-  split::SplitVector<key_type> evens;
-  for (size_t i = 0; i < N; i += 2) evens.push_back((key_type)i);
-  b.erase(evens.data(), evens.size());
-  EXPECT_TRUE(b.tombstone_count() == N / 2);
-  EXPECT_TRUE(b.tombstone_ratio() == (float)(N / 2) / (float)(1 << 13));
-  EXPECT_TRUE(a.tombstone_ratio() == 0.0f);
-  auto odd_valid = [] __host__ __device__(hash_pair<key_type, val_type> & e) -> bool {
-    return e.first != 0xFFFFFFFFu && e.first != 0xFFFFFFFEu && e.second % 2 == 1;
-  };
-  vector e1, e2;
-  split::SplitVector<key_type> k1, k2;
-  b.extractLoop(e1);
-  b.extractPatternLoop(e2, odd_valid);
-  b.extractAllKeysLoop(k1);
-  b.extractKeysByPatternLoop(k2, odd_valid);
-  EXPECT_TRUE(e1.size() == N / 2 && e2.size() == N / 2 && k1.size() == N / 2 && k2.size() == N / 2);
-  bool ok = true;
-  for (auto& e : e1) ok = ok && e.first % 2 == 1 && e.second == e.first;
-  for (size_t i = 0; i < e2.size() && i < e1.size(); ++i) ok = ok && e2[i] == e1[i];  // both in bucket order
-  for (size_t i = 0; i < k1.size() && i < e1.size(); ++i) ok = ok && k1[i] == e1[i].first && k2[i] == k1[i];
-  EXPECT_TRUE(ok);
-  b.memAdvise(cudaMemAdviseSetPreferredLocation, 0);
-  b.streamAttach(0);
-  b.stats();
-  hashmap tiny(4);
-  tiny.insert(src.data(), 3, 1.0f);
-  tiny.dump_buckets();
-  EXPECT_TRUE(tiny.size() == 3);
-}
-
 struct test_t {
   uint32_t num, flag;
 };
@@ -285,10 +166,6 @@ int main() {
   for (int p = 10; p <= 16; p += 3) test_hashmap_4(p);
   test_duplicate_insertion();
   test_extract_rules();
-  test_copy_metadata();
-  test_custom_sentinels();
-  test_arena_and_key_overloads();
-  test_more_host_methods();
   for (size_t s = 32; s < 3000; s += 37) EXPECT_TRUE(compaction_flags(s));
   for (int p = 5; p < 20; p += 2) EXPECT_TRUE(compaction_flags(size_t(1) << p));
   for (int p = 2; p < 18; ++p) EXPECT_TRUE(scan_iota(size_t(1) << p));
