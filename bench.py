@@ -265,6 +265,80 @@ def cpu_batched(w: dict, gpu_out=None, threads: int | None = None, reps: int = 2
     return r
 
 
+SERVE_FILL = 0xA5A5A5A5A5A5A5A5  # query-output pre-fill of the CPU replay (misses leave it)
+
+
+def cpu_serving(tr: dict, gpu_out=None, threads: int | None = None, max_lf: float = 0.8) -> dict:
+    """CPU baseline of the serving workload: every map an oracle serial map (the reference's CPU path restated),
+    maps dealt round-robin to host threads, each thread replaying its maps' requests in admission order (the
+    trace's order) with the server's maintenance rule: before an insert that would take keys plus tombstones past
+    max_lf, rehash (dropping tombstones, growing while the live keys need it). The initial inserts are not timed,
+    as on the GPU. If gpu_out (the serving run's query outputs, 64-bit) is given, it is compared with the CPU's
+    at every query position where the CPU found the key (the GPU buffer is not pre-filled, so misses are not
+    compared)."""
+    import oracle
+    from concurrent.futures import ThreadPoolExecutor
+    t = threads or host_threads()
+    sps = tr["size_powers"]
+    nm = len(sps)
+    io, ro = tr["init_offsets"].astype(np.int64), tr["req_offsets"].astype(np.int64)
+    rmap, rop = tr["req_map"], tr["req_op"]
+    ik, iv, rk, rv = (np.ascontiguousarray(tr[k]).view(np.uint64)
+                      for k in ("init_keys", "init_vals", "req_keys", "req_vals"))
+    out = np.full(len(rk), SERVE_FILL, np.uint64)
+    order = np.argsort(rmap, kind="stable")
+    starts = np.searchsorted(rmap[order], np.arange(nm + 1))
+    maps = [None] * nm
+    growths = [0] * t
+
+    def init(tid):
+        for m in range(tid, nm, t):
+            om = oracle.OracleMap(int(sps[m]), 8)
+            om.insert(ik[io[m]:io[m + 1]], iv[io[m]:io[m + 1]], 0.0)
+            maps[m] = om
+
+    def replay(tid):
+        for m in range(tid, nm, t):
+            om = maps[m]
+            for i in order[starts[m]:starts[m + 1]].tolist():
+                a, b = int(ro[i]), int(ro[i + 1])
+                op = int(rop[i])
+                if op == 0:
+                    inf = om.info()
+                    sp = inf["size_power"]
+                    if inf["fill"] + inf["tombstones"] + (b - a) > max_lf * (1 << sp):
+                        while inf["fill"] + (b - a) > max_lf * (1 << sp):
+                            sp += 1
+                        om.resize(sp)
+                        growths[tid] += 1
+                    om.insert(rk[a:b], rv[a:b], 0.0)
+                elif op == 1:
+                    om.retrieve(rk[a:b], out[a:b])
+                else:
+                    om.erase(rk[a:b])
+
+    with ThreadPoolExecutor(max_workers=t) as ex:
+        list(ex.map(init, range(t)))
+        t0 = time.perf_counter()
+        list(ex.map(replay, range(t)))
+        dt = time.perf_counter() - t0
+    keys = int(ro[-1])
+    r = {"ms": round(dt * 1e3, 1), "Mkeys_s": round(keys / dt / 1e6, 1), "threads": t, "kind": "port",
+         "rehashes": int(sum(growths)),
+         "sample": "the whole trace (every request), no arrival times: one serial map per map, maps dealt "
+                   "round-robin to host threads"}
+    if gpu_out is not None:
+        q = np.zeros(len(rk), bool)
+        for i in np.flatnonzero(rop == 1).tolist():
+            q[int(ro[i]):int(ro[i + 1])] = True
+        hit = q & (out != np.uint64(SERVE_FILL))
+        g = np.asarray(gpu_out).view(np.uint64)
+        r["query_hits_compared"] = int(hit.sum())
+        r["query_hits_equal_gpu"] = bool(np.array_equal(out[hit], g[hit]))
+    del maps
+    return r
+
+
 def cpu_streaming(log_n: int = 24, threads: int | None = None, reps: int = 3) -> dict:
     """CPU baseline of the streaming primitives on a bounded sample of 2^log_n u32 (uniform; scan input in
     [0, 16)): the oracle's serial copy_if with (x % 100) < s, s = 1/50/99, and its serial exclusive scan, on one
@@ -457,7 +531,8 @@ def run_serving(args, dev):
                         f"past LF 0.8; {n_req} Poisson requests of log-uniform 1..2^16 keys, insert/query/erase "
                         f"20/70/10, queries 80% present",
             "keys_per_run": total_keys, "initial_keys": int(io[-1]), "rates": results, "generate_s": round(gen_s, 1),
-            "latency": "arrival (host clock) to the end of the request's round (CUDA event on the serving stream)"}
+            "latency": "arrival (host clock) to the end of the request's round (CUDA event on the serving stream)",
+            "cpu_baseline": _guarded(lambda: cpu_serving(tr, out.cpu().numpy()))}
 
 
 def _ev_time(stream, fn, reps=3):

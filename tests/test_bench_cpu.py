@@ -65,3 +65,37 @@ def test_cpu_batched_baseline_against_a_dict_model():
     bad = expect.copy()
     bad[len(bad) // 2] ^= 1
     assert bench.cpu_batched(w, bad, threads=2, reps=1)["query_outputs_equal_gpu"] is False
+
+
+def test_cpu_serving_baseline_against_a_dict_model():
+    sys.path.insert(0, str(ROOT))
+    import numpy as np
+    import bench
+    from hashinator_gb300 import workloads
+
+    nm, nr = 6, 300
+    tr = workloads.serving_trace(nm, nr, 21, init_log=(4.0, 8.0), size_log=(0.0, 7.0), width=8)
+    io, ro = tr["init_offsets"], tr["req_offsets"]
+    d = [dict(zip(tr["init_keys"][io[m]:io[m + 1]].tolist(), tr["init_vals"][io[m]:io[m + 1]].tolist()))
+         for m in range(nm)]
+    model = np.zeros(len(tr["req_keys"]), np.uint64)  # a miss may hold anything in the GPU's buffer
+    hits = 0
+    for i in range(nr):
+        m, op = int(tr["req_map"][i]), int(tr["req_op"][i])
+        ks = tr["req_keys"][ro[i]:ro[i + 1]].tolist()
+        if op == 0:
+            d[m].update(zip(ks, tr["req_vals"][ro[i]:ro[i + 1]].tolist()))
+        elif op == 1:
+            for j, k in enumerate(ks):
+                if k in d[m]:
+                    model[ro[i] + j] = d[m][k]
+                    hits += 1
+        else:
+            for k in ks:
+                d[m].pop(k, None)
+    r = bench.cpu_serving(tr, model.view(np.int64), threads=3)
+    assert r["query_hits_equal_gpu"] is True and r["query_hits_compared"] == hits > 0
+    assert r["rehashes"] > 0  # the trace grows some maps
+    bad = model.copy()
+    bad[np.flatnonzero(bad)[hits // 2]] ^= np.uint64(1)
+    assert bench.cpu_serving(tr, bad, threads=2)["query_hits_equal_gpu"] is False
