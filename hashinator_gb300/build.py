@@ -69,7 +69,7 @@ def build_lib(verbose: bool = False, force: bool = False) -> Path:
         msg = "\n".join(f"--- {s}\n{o}" for s, o in failed)
         raise RuntimeError(f"nvcc failed:\n{msg}")
     if force or _stale(LIB, objs):
-        cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-o", str(LIB), *map(str, objs)]
+        cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-o", str(LIB), *map(str, objs), "-ldl"]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)

@@ -634,6 +634,7 @@ hx_status hx_batch_bucket_data(hx_batch* b, uint32_t map, void** d_buckets, uint
 }
 
 hx_status hx_batch_plan_create(hx_batch* b, const hx_batch_work* w, hx_batch_plan** out, hx_stream stream) {
+  HX_RANGE("hx_batch_plan_create");
   if (!b || !w || !out) return HX_ERR_INVALID_ARG;
   *out = nullptr;
   const unsigned nm = b->n_maps;
@@ -733,6 +734,7 @@ static void account_inserts(hx_batch_plan* p) {
 }
 
 hx_status hx_batch_run(hx_batch_plan* p, hx_stream stream) {
+  HX_RANGE("hx_batch_run");
   if (!p) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   account_inserts(p);
@@ -740,6 +742,7 @@ hx_status hx_batch_run(hx_batch_plan* p, hx_stream stream) {
 }
 
 hx_status hx_batch_run_graph(hx_batch_plan* p, hx_stream stream) {
+  HX_RANGE("hx_batch_run_graph");
   if (!p) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (!p->graph_exec) {
@@ -764,6 +767,7 @@ hx_status hx_batch_run_graph(hx_batch_plan* p, hx_stream stream) {
 }
 
 hx_status hx_batch_run_per_map(hx_batch_plan* p, hx_stream stream) {
+  HX_RANGE("hx_batch_run_per_map");
   if (!p) return HX_ERR_INVALID_ARG;
   hx_batch* b = p->b;
   cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -5,7 +5,30 @@
 #include <cuda_runtime.h>
 #include "../../include/hx.h"
 
+// NVTX ranges name each C-ABI call in Nsight Systems timelines and for
+// `ncu --nvtx` filters. NVTX v3 is header-only; with no tool attached a range
+// costs one call that returns at once. Build with -DHX_NVTX=0 to compile
+// them out.
+#ifndef HX_NVTX
+#define HX_NVTX 1
+#endif
+#if HX_NVTX
+#include <nvtx3/nvToolsExt.h>
+#endif
+
 namespace hx {
+
+#if HX_NVTX
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define HX_RANGE(name) ::hx::NvtxRange hx_nvtx_range_(name)
+#else
+#define HX_RANGE(name) ((void)0)
+#endif
 
 // Records the CUDA error for hx_last_cuda_error() and maps it to a status.
 hx_status cuda_status(cudaError_t e);

@@ -834,6 +834,7 @@ hx_status hx_map_destroy(hx_map* m) {
 
 hx_status hx_insert(hx_map* m, const void* d_keys, const void* d_vals, uint64_t n, float target_lf,
                     hx_stream stream) {
+  HX_RANGE("hx_insert");
   if (!valid_map(m)) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   HX_CUDA(cudaMemsetAsync(&m->info->err, 0, sizeof(int), s));  // err = success (hashers.h:50)
@@ -848,6 +849,7 @@ hx_status hx_insert(hx_map* m, const void* d_keys, const void* d_vals, uint64_t 
 }
 
 hx_status hx_insert_index(hx_map* m, const void* d_keys, uint64_t n, float target_lf, hx_stream stream) {
+  HX_RANGE("hx_insert_index");
   if (!valid_map(m)) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   HX_CUDA(cudaMemsetAsync(&m->info->err, 0, sizeof(int), s));
@@ -862,6 +864,7 @@ hx_status hx_insert_index(hx_map* m, const void* d_keys, uint64_t n, float targe
 }
 
 hx_status hx_insert_pairs(hx_map* m, const void* d_pairs, uint64_t n, float target_lf, hx_stream stream) {
+  HX_RANGE("hx_insert_pairs");
   if (!valid_map(m)) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   HX_CUDA(cudaMemsetAsync(&m->info->err, 0, sizeof(int), s));
@@ -876,6 +879,7 @@ hx_status hx_insert_pairs(hx_map* m, const void* d_pairs, uint64_t n, float targ
 }
 
 hx_status hx_retrieve(hx_map* m, const void* d_keys, void* d_vals, uint64_t n, hx_stream stream) {
+  HX_RANGE("hx_retrieve");
   if (!valid_map(m)) return HX_ERR_INVALID_ARG;
   if (n == 0) return HX_OK;
   if (!d_keys || !d_vals) return HX_ERR_INVALID_ARG;
@@ -885,6 +889,7 @@ hx_status hx_retrieve(hx_map* m, const void* d_keys, void* d_vals, uint64_t n, h
 }
 
 hx_status hx_retrieve_pairs(hx_map* m, void* d_pairs, uint64_t n, hx_stream stream) {
+  HX_RANGE("hx_retrieve_pairs");
   if (!valid_map(m)) return HX_ERR_INVALID_ARG;
   if (n == 0) return HX_OK;
   if (!d_pairs) return HX_ERR_INVALID_ARG;
@@ -894,6 +899,7 @@ hx_status hx_retrieve_pairs(hx_map* m, void* d_pairs, uint64_t n, hx_stream stre
 }
 
 hx_status hx_erase(hx_map* m, const void* d_keys, uint64_t n, hx_stream stream) {
+  HX_RANGE("hx_erase");
   if (!valid_map(m)) return HX_ERR_INVALID_ARG;
   if (n == 0) return HX_OK;
   if (!d_keys) return HX_ERR_INVALID_ARG;
@@ -903,6 +909,7 @@ hx_status hx_erase(hx_map* m, const void* d_keys, uint64_t n, hx_stream stream) 
 }
 
 hx_status hx_clean_tombstones(hx_map* m, hx_stream stream) {
+  HX_RANGE("hx_clean_tombstones");
   if (!valid_map(m)) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   std::lock_guard<std::mutex> g(m->mu);
@@ -939,20 +946,24 @@ hx_status hx_clean_tombstones(hx_map* m, hx_stream stream) {
 
 hx_status hx_extract_pattern(hx_map* m, const hx_pred* pred, void* d_out, uint64_t capacity, uint64_t* d_count,
                              uint64_t* h_count, hx_stream stream) {
+  HX_RANGE("hx_extract_pattern");
   return extract<false>(m, pred, d_out, capacity, d_count, h_count, stream);
 }
 
 hx_status hx_extract_keys(hx_map* m, const hx_pred* pred, void* d_out_keys, uint64_t capacity, uint64_t* d_count,
                           uint64_t* h_count, hx_stream stream) {
+  HX_RANGE("hx_extract_keys");
   return extract<true>(m, pred, d_out_keys, capacity, d_count, h_count, stream);
 }
 
 hx_status hx_resize(hx_map* m, int new_size_power, hx_stream stream) {
+  HX_RANGE("hx_resize");
   if (!valid_map(m)) return HX_ERR_INVALID_ARG;
   return rehash(m, new_size_power, static_cast<cudaStream_t>(stream));
 }
 
 hx_status hx_clear(hx_map* m, hx_stream stream) {
+  HX_RANGE("hx_clear");
   if (!valid_map(m)) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   hx_status st = fill_empty(m, m->buckets, nslots(m), s);
@@ -963,6 +974,7 @@ hx_status hx_clear(hx_map* m, hx_stream stream) {
 }
 
 hx_status hx_resize_to_lf(hx_map* m, float target_lf, hx_stream stream) {
+  HX_RANGE("hx_resize_to_lf");
   if (!valid_map(m) || !(target_lf > 0.0f)) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   DInfo di;
@@ -976,6 +988,7 @@ hx_status hx_resize_to_lf(hx_map* m, float target_lf, hx_stream stream) {
 }
 
 hx_status hx_perform_cleanup_tasks(hx_map* m, hx_stream stream) {
+  HX_RANGE("hx_perform_cleanup_tasks");
   if (!valid_map(m)) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   DInfo di;
@@ -994,6 +1007,7 @@ hx_status hx_perform_cleanup_tasks(hx_map* m, hx_stream stream) {
 }
 
 hx_status hx_get_info(hx_map* m, hx_info* out, hx_stream stream) {
+  HX_RANGE("hx_get_info");
   if (!valid_map(m) || !out) return HX_ERR_INVALID_ARG;
   DInfo di;
   hx_status st = read_info(m, &di, static_cast<cudaStream_t>(stream));

@@ -55,6 +55,7 @@ using namespace hx;
 
 extern "C" hx_status hx_exclusive_scan_u32_noalloc(const uint32_t* d_in, uint32_t* d_out, uint64_t n,
                                                    hx_stream stream) {
+  HX_RANGE("hx_exclusive_scan_u32_noalloc");
   if (n == 0) return HX_OK;
   if (!d_in || !d_out) return HX_ERR_INVALID_ARG;
   if (n > HX_NOALLOC_SCAN_MAX_N) return HX_ERR_INVALID_ARG;  // beyond the fixed scratch: nothing launched

@@ -201,6 +201,7 @@ hx_status hx_scratch_bytes(int op, uint64_t n, uint64_t* bytes) {
 
 hx_status hx_exclusive_scan_u32(const uint32_t* d_in, uint32_t* d_out, uint64_t n, void* d_scratch,
                                 uint64_t scratch_bytes, hx_stream stream) {
+  HX_RANGE("hx_exclusive_scan_u32");
   if (n == 0) return HX_OK;
   if (!d_in || !d_out) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -217,6 +218,7 @@ hx_status hx_exclusive_scan_u32(const uint32_t* d_in, uint32_t* d_out, uint64_t 
 hx_status hx_copy_if(const void* d_in, void* d_out, uint64_t n, int elem_bytes, const hx_pred* pred,
                      uint64_t capacity, uint64_t* d_count, uint64_t* h_count, void* d_scratch,
                      uint64_t scratch_bytes, hx_stream stream) {
+  HX_RANGE("hx_copy_if");
   if (!pred || (n && (!d_in || !d_out))) return HX_ERR_INVALID_ARG;
   if (pred->op == HX_PRED_MOD_LT && pred->a == 0) return HX_ERR_INVALID_ARG;
   if (pred->op > HX_PRED_NOT_HOME) return HX_ERR_INVALID_ARG;

@@ -538,6 +538,7 @@ hx_status hx_server_submit(hx_server* sv, const hx_request* reqs, uint32_t count
 static hx_status server_step(hx_server* sv, uint32_t* launched);
 
 hx_status hx_server_step(hx_server* sv, uint32_t* launched) {
+  HX_RANGE("hx_server_step");
   if (!sv) return HX_ERR_INVALID_ARG;
   const uint64_t t0 = now_ns();
   hx_status st = server_step(sv, launched);
@@ -838,6 +839,7 @@ hx_status hx_server_memory(hx_server* sv, uint64_t* used, uint64_t* budget) {
 
 hx_status hx_server_run_trace(hx_server* sv, const hx_request* reqs, const uint64_t* arrival_ns, uint32_t count,
                               uint64_t* complete_ns, int32_t* status, uint64_t* t_start_ns) {
+  HX_RANGE("hx_server_run_trace");
   if (!sv || (count && (!reqs || !arrival_ns || !complete_ns || !status))) return HX_ERR_INVALID_ARG;
   for (uint32_t i = 0; i < count; ++i) {
     complete_ns[i] = 0;
