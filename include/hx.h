@@ -338,7 +338,11 @@ hx_status hx_batch_inject_stall(hx_batch_plan* plan, uint32_t map, int phase, in
  * whose load factor would pass max_load_factor is grown by an on-device
  * rehash; tables are admitted against memory_budget_bytes, and an insert
  * that cannot grow its table within the budget completes with HX_ERR_OOM.
- * One host thread drives a server. */
+ * One host thread drives a server. Tables live in the device's default
+ * stream-ordered memory pool, and hx_server_create sets that pool's release
+ * threshold to keep freed memory (cudaMemPoolAttrReleaseThreshold = max), so
+ * that growth does not return memory to the driver at every synchronisation;
+ * the setting belongs to the process and stays after hx_server_destroy. */
 typedef struct hx_server hx_server;
 enum { HX_OP_INSERT = 0, HX_OP_QUERY = 1, HX_OP_ERASE = 2 };
 typedef struct hx_request {
