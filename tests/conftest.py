@@ -53,6 +53,11 @@ def golden_cases():
     return sorted(p.stem for p in GOLDEN.glob("*.npz"))
 
 
+def golden_extra_cases():
+    """Edge-case fixtures (tests/golden/extra/), loaded as "extra/<name>"."""
+    return sorted(f"extra/{p.stem}" for p in (GOLDEN / "extra").glob("*.npz"))
+
+
 def load_golden(name):
     import numpy as np
     with np.load(GOLDEN / f"{name}.npz") as z:

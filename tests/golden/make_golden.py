@@ -6,7 +6,8 @@ from hashinator_gb300.workloads and stores inputs and outputs as compressed
 .npz files. Needs the reference source tree (only present where the fixtures
 are made); the fixtures themselves are committed and read by the tests.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every fixture
+    python tests/golden/make_golden.py --extra    # only the edge cases in tests/golden/extra/
 """
 from __future__ import annotations
 
@@ -34,6 +35,18 @@ CASES = {
     "u32_lf090_sp12": (4, 12, int(0.9 * 4096), 0.5, 0.30, 13),
     "u64_lf050_sp12": (8, 12, 2048, 0.5, 0.30, 14),
     "u64_lf090_sp12": (8, 12, int(0.9 * 4096), 0.5, 0.30, 15),
+}
+
+# Edge cases, written to tests/golden/extra/: the remaining width x load-factor
+# pair, queries that all hit or all miss, erasing every key, and tiny tables.
+EXTRA_CASES = {
+    "u64_lf075_sp12": (8, 12, 3072, 0.5, 0.30, 16),
+    "u32_hit100_sp10": (4, 10, 400, 1.0, 0.50, 17),
+    "u32_hit0_sp10": (4, 10, 400, 0.0, 0.0, 18),
+    "u32_erase_all_sp8": (4, 8, 100, 0.5, 1.0, 19),
+    "u32_tiny_sp2": (4, 2, 3, 0.5, 0.34, 20),
+    "u64_tiny_sp3": (8, 3, 6, 0.5, 0.5, 22),
+    "u64_ragged_sp11": (8, 11, 1001, 0.5, 0.27, 23),
 }
 
 
@@ -70,12 +83,14 @@ def run_driver(width: int, sp: int, keys, vals, q, e) -> dict:
     return out
 
 
-def make_case(name: str, width: int, sp: int, n: int, hit: float, erase: float, seed: int) -> None:
+def make_case(name: str, width: int, sp: int, n: int, hit: float, erase: float, seed: int, out_dir: Path = OUT) -> None:
     keys, vals, q, e = workloads.map_workload(n, width, seed, hit_frac=hit, n_queries=2 * n if hit == 0.5 and
                                               name.startswith("u32_lf050") else n, erase_frac=erase)
     res = run_driver(width, sp, keys, vals, q, e)
-    np.savez_compressed(OUT / f"{name}.npz", key_bytes=width, size_power=sp, fill_pattern=np.uint64(FILL[width]),
-                        seed=seed, keys=keys, vals=vals, queries=q, erase=e, **res)
+    out_dir.mkdir(exist_ok=True)
+    np.savez_compressed(out_dir / f"{name}.npz", key_bytes=width, size_power=sp,
+                        fill_pattern=np.uint64(FILL[width]), seed=seed, keys=keys, vals=vals, queries=q, erase=e,
+                        **res)
     print(f"{name}: n={n} size={res['size_after_insert']} erased={res['n_erased']} "
           f"tomb={res['tombstones_after_erase']} sp_final={res['size_power_final']}")
 
@@ -100,6 +115,9 @@ def make_duplicates() -> None:
 if __name__ == "__main__":
     if not DRIVER.exists():
         sys.exit(f"{DRIVER} missing: run `make -C oracle` where the reference source tree is present")
-    for nm, args in CASES.items():
-        make_case(nm, *args)
-    make_duplicates()
+    if "--extra" not in sys.argv[1:]:
+        for nm, args in CASES.items():
+            make_case(nm, *args)
+        make_duplicates()
+    for nm, args in EXTRA_CASES.items():
+        make_case(nm, *args, out_dir=OUT / "extra")

@@ -4,14 +4,14 @@ inputs; the oracle must reproduce them exactly."""
 import numpy as np
 import pytest
 
-from conftest import golden_cases, load_golden
+from conftest import golden_cases, golden_extra_cases, load_golden
 
 
 def _dt(g):
     return np.uint32 if int(g["key_bytes"]) == 4 else np.uint64
 
 
-@pytest.mark.parametrize("name", golden_cases())
+@pytest.mark.parametrize("name", golden_cases() + golden_extra_cases())
 def test_oracle_matches_reference_cpu_build(oracle_mod, name):
     g = load_golden(name)
     kb, sp, dt = int(g["key_bytes"]), int(g["size_power"]), _dt(g)
@@ -45,7 +45,7 @@ def test_oracle_matches_reference_cpu_build(oracle_mod, name):
     np.testing.assert_array_equal(v, g["map_vals"])
 
 
-@pytest.mark.parametrize("name", golden_cases())
+@pytest.mark.parametrize("name", golden_cases() + golden_extra_cases())
 def test_oracle_clean_and_rehash_keep_mapping(oracle_mod, name):
     g = load_golden(name)
     kb, sp = int(g["key_bytes"]), int(g["size_power"])
