@@ -96,7 +96,7 @@ __device__ __forceinline__ bool wait_zero(const unsigned* p) {
 template <class P, int G, int BLOCK>
 // The round is bound by memory-level parallelism (random probes of many small
 // tables), not by DRAM bytes: capping registers so that 48 warps fit per SM
-// (some spills to L1) took it from 4.55 to 3.2 ms against 20 warps at 96
+// (some spills to L1) took it from about 4.5 to 3.2 ms against 20 warps at 96
 // registers (sweep of 20/24/32/40/48/64 warps on GB300).
 #ifndef HX_BATCH_MIN_WARPS
 #define HX_BATCH_MIN_WARPS 48
