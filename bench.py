@@ -199,6 +199,30 @@ def cpu_insert_query(width: int = 4, log_n: int = 24, threads: int = 1, reps: in
     return 2 * n / (t2 - t0) / 1e6, n / (t1 - t0) / 1e6, n / (t2 - t1) / 1e6, t2 - t0
 
 
+def host_cpu() -> dict:
+    """The host the CPU baseline ran on: logical CPUs and the CPU model (lscpu, else /proc/cpuinfo)."""
+    import platform
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().lower().startswith("model name"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except Exception:  # noqa: BLE001
+        pass
+    if not model:
+        try:
+            for ln in Path("/proc/cpuinfo").read_text().splitlines():
+                if ln.lower().startswith("model name"):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+        except Exception:  # noqa: BLE001
+            pass
+    return {"nproc": os.cpu_count(), "cpu_model": model or platform.processor() or "unknown",
+            "arch": platform.machine()}
+
+
 def host_threads() -> int:
     """Host threads for the CPU baseline: the largest power of two not above the core count."""
     c = os.cpu_count() or 1
@@ -215,7 +239,7 @@ def cpu_baseline(width: int = 4, log_n: int = 24):
                       f"{t} serial maps (the reference's CPU path restated), keys sharded by the top bits of their "
                       f"home bucket; insert {vi:.1f} Mkeys/s, query {vq:.1f} Mkeys/s",
             "single_core": {"value": round(v1, 3), "insert_Mkeys_s": round(vi1, 1), "query_Mkeys_s": round(vq1, 1)},
-            "seconds": round(secs + secs1, 3), "streaming": _guarded(cpu_streaming)}
+            "seconds": round(secs + secs1, 3), "host": _guarded(host_cpu), "streaming": _guarded(cpu_streaming)}
 
 
 def _guarded(fn):
@@ -704,7 +728,8 @@ def run_reference(args):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": DATA,
             "config": config,
-            "cpu_baseline": {"value": round(v, 3), "unit": "Mkeys/s", "cores": t, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": round(v, 3), "unit": "Mkeys/s", "cores": t, "kind": "port", "sample": sample,
+                             "host": _guarded(host_cpu)},
             "e2e": {"value": round(v, 3), "unit": "Mkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
