@@ -53,3 +53,28 @@ def test_no_cpu_fallback_in_product():
     for p in (ROOT / "hashinator_gb300").rglob("*.py"):
         src = p.read_text()
         assert "import oracle" not in src and "from oracle" not in src, p
+
+
+def test_null_handles_and_outputs_are_rejected(hx):
+    """Every entry point that takes a map, batch, plan or server handle returns HX_ERR_INVALID_ARG for a NULL
+    handle before any device work, and the create calls reject a NULL output and bad sizes (no GPU here)."""
+    lib = hx.lib()
+    no_handle = {"hx_status_string", "hx_last_cuda_error", "hx_kernel_launch_count", "hx_set_l2_fetch_granularity",
+                 "hx_diag_random_access", "hx_scratch_bytes", "hx_exclusive_scan_u32", "hx_copy_if",
+                 "hx_map_create", "hx_batch_create", "hx_server_create", "hx_exclusive_scan_u32_noalloc"}
+    names = sorted((set(hx._SIGS) | set(hx._EXTRA_SIGS)) - no_handle)
+    assert len(names) >= 40
+    for n in names:
+        f = getattr(lib, n)
+        args = [0 if isinstance(t, type) and issubclass(t, (ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64,
+                                                               ctypes.c_int32, ctypes.c_float)) else None
+                for t in f.argtypes]
+        assert f(*args) == hx.HX_ERR_INVALID_ARG, n
+    sp = (ctypes.c_int32 * 2)(10, 10)
+    h = ctypes.c_void_p()
+    assert lib.hx_map_create(None, 4, 4, 10, None) == hx.HX_ERR_INVALID_ARG
+    assert lib.hx_batch_create(None, 2, sp, 4, 4, None) == hx.HX_ERR_INVALID_ARG
+    assert lib.hx_batch_create(ctypes.byref(h), 0, sp, 4, 4, None) == hx.HX_ERR_INVALID_ARG
+    assert lib.hx_server_create(None, 8, 1 << 30, 0.8, 4, 16, 1 << 20, 2) == hx.HX_ERR_INVALID_ARG
+    assert lib.hx_server_create(ctypes.byref(h), 8, 1 << 30, 0.0, 4, 16, 1 << 20, 2) == hx.HX_ERR_INVALID_ARG
+    assert lib.hx_exclusive_scan_u32_noalloc(None, None, (1 << 28) + 1, None) == hx.HX_ERR_INVALID_ARG
