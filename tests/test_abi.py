@@ -78,3 +78,32 @@ def test_null_handles_and_outputs_are_rejected(hx):
     assert lib.hx_server_create(None, 8, 1 << 30, 0.8, 4, 16, 1 << 20, 2) == hx.HX_ERR_INVALID_ARG
     assert lib.hx_server_create(ctypes.byref(h), 8, 1 << 30, 0.0, 4, 16, 1 << 20, 2) == hx.HX_ERR_INVALID_ARG
     assert lib.hx_exclusive_scan_u32_noalloc(None, None, (1 << 28) + 1, None) == hx.HX_ERR_INVALID_ARG
+
+
+def test_scratch_sizes_and_undersized_caller_scratch(hx):
+    """hx_scratch_bytes: the scan needs a 256-byte header and one 8-byte status per 4096-element tile; copy_if
+    needs at least as much plus a 256-byte count area, never shrinking as n grows. A caller buffer smaller than
+    the need is rejected before any device work: every call here is one that must be rejected, so the fake
+    pointers are never dereferenced."""
+    lib = hx.lib()
+    b = ctypes.c_uint64()
+
+    def need(op, n):
+        assert lib.hx_scratch_bytes(op, n, ctypes.byref(b)) == hx.HX_OK
+        return b.value
+
+    for n in (0, 1, 4095, 4096, 4097, 1 << 20, (1 << 28) + 3):
+        assert need(hx.SCRATCH_SCAN, n) == 256 + 8 * max(1, -(-n // 4096))
+    prev = 0
+    for n in (0, 1, 100, 5000, 1 << 16, 1 << 20, 1 << 24):
+        c = need(hx.SCRATCH_COPY_IF, n)
+        assert c >= prev and c >= 256 + 8 + 256
+        prev = c
+    fake = ctypes.c_void_p(256)
+    n = 5000
+    p = hx.Pred.mod_lt(100, 50).c()
+    # 256 bytes is below every element width's need (a header, at least one status, the count area)
+    for elem in (4, 8, 16):
+        assert lib.hx_copy_if(fake, fake, n, elem, ctypes.byref(p), n, None, None, fake, 256, None) == \
+            hx.HX_ERR_INVALID_ARG
+    assert lib.hx_exclusive_scan_u32(fake, fake, n, fake, need(hx.SCRATCH_SCAN, n) - 1, None) == hx.HX_ERR_INVALID_ARG
