@@ -107,3 +107,23 @@ def test_scratch_sizes_and_undersized_caller_scratch(hx):
         assert lib.hx_copy_if(fake, fake, n, elem, ctypes.byref(p), n, None, None, fake, 256, None) == \
             hx.HX_ERR_INVALID_ARG
     assert lib.hx_exclusive_scan_u32(fake, fake, n, fake, need(hx.SCRATCH_SCAN, n) - 1, None) == hx.HX_ERR_INVALID_ARG
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/hx.h compiles as C99 with warnings as errors, so C code and any FFI generator can use it."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        import pytest
+        pytest.skip("no C compiler")
+    src = tmp_path / "use_hx.c"
+    src.write_text('#include "hx.h"\n'
+                   "int main(void) {\n"
+                   "  hx_map* m = 0; hx_info info; hx_pred p = {HX_PRED_MOD_LT, HX_FIELD_ELEM, 0, 0, 100, 50};\n"
+                   "  (void)m; (void)info; (void)p;\n"
+                   "  return hx_status_string(HX_OK) ? 0 : 1;\n"
+                   "}\n")
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", str(ROOT / "include"),
+                        "-c", str(src), "-o", str(tmp_path / "use_hx.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
