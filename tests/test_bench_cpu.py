@@ -100,3 +100,24 @@ def test_cpu_serving_baseline_against_a_dict_model():
     bad = model.copy()
     bad[np.flatnonzero(bad)[hits // 2]] ^= np.uint64(1)
     assert bench.cpu_serving(tr, bad, threads=2)["query_hits_equal_gpu"] is False
+
+
+def test_reference_arm_under_two_ranks():
+    """Launched like the multi-GPU runs (torch.distributed.run, 2 processes), the reference arm prints one JSON
+    line from rank 0 with n_gpus = 2 and every rank exits 0."""
+    import os
+    import socket
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+                        "--master-addr", "127.0.0.1", "--master-port", str(port), str(ROOT / "bench.py"),
+                        "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3"],
+                       cwd=ROOT, capture_output=True, text=True, timeout=900, env=env)
+    assert r.returncode == 0, r.stderr[-3000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
