@@ -60,6 +60,7 @@ class Info(ctypes.Structure):
         ("tombstone_counter", ctypes.c_uint64),
         ("max_probe", ctypes.c_uint64),
         ("bucket_count", ctypes.c_uint64),
+        ("last_clean_moved", ctypes.c_uint64),
     ]
 
 

@@ -1021,6 +1021,7 @@ hx_status hx_get_info(hx_map* m, hx_info* out, hx_stream stream) {
   r = (r + 31) / 32 * 32;  // nextOverflow(overflow, 32), common.h:54-57
   out->current_max_bucket_overflow = r < 32 ? 32 : r;
   out->bucket_count = nslots(m);
+  out->last_clean_moved = di.moved;
   return HX_OK;
 }
 

@@ -12,6 +12,8 @@
 // from module load until the process exits. All calls share it, so calls
 // that overlap on the GPU corrupt each other's results: order them on one
 // stream (or otherwise serialise them).
+#include <cuda.h>
+
 #include <mutex>
 
 #include "hx_host.h"
@@ -28,23 +30,61 @@ static_assert(256 + 8 * kNoAllocTiles <= HX_NOALLOC_SCAN_SCRATCH_BYTES, "ticket/
 // the largest scan, 2^28 elements).
 static __device__ __align__(256) unsigned char g_noalloc_scan_scratch[HX_NOALLOC_SCAN_SCRATCH_BYTES];
 
-// Device address of the array, looked up once per device with that device
-// current. In host code the array's name is only a host-side stand-in, so the
-// address must come from cudaGetSymbolAddress.
+// The current context's driver-assigned id (unique for the life of the
+// process), through the runtime's driver entry points so that libhx does not
+// link libcuda. 0 when the driver does not provide it.
+static unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
+
+// Device address of the array in the current device's context. In host code
+// the array's name is only a host-side stand-in, so the address comes from
+// cudaGetSymbolAddress, called with the device current. It is looked up once
+// per device and context: a cudaDeviceReset ends the context, the module is
+// loaded again in the next one and the array may then sit elsewhere, so an
+// address is reused only while the context that it was looked up in is the
+// current one (when the driver cannot name contexts, it is looked up on
+// every call).
 static void* noalloc_scratch(int dev, cudaError_t* err) {
   static std::mutex mu;
   static void* addr[64] = {nullptr};
+  static unsigned long long ctx_of[64] = {0};
   *err = cudaSuccess;
   if (dev < 0 || dev >= 64) {
     *err = cudaErrorInvalidDevice;
     return nullptr;
   }
+  // Make the device's primary context current (cudaSetDevice initialises it),
+  // so that the id below names the context the kernel will run in.
+  if ((*err = cudaSetDevice(dev)) != cudaSuccess) return nullptr;
+  const unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> g(mu);
-  if (!addr[dev]) {
+  if (!addr[dev] || ctx == 0 || ctx_of[dev] != ctx) {
     void* p = nullptr;
     *err = cudaGetSymbolAddress(&p, g_noalloc_scan_scratch);
     if (*err != cudaSuccess) return nullptr;
     addr[dev] = p;
+    ctx_of[dev] = ctx;
   }
   return addr[dev];
 }

@@ -338,6 +338,7 @@ struct hx_server {
   hx::SMap* d_maps = nullptr;
   hx::DInfo* d_info = nullptr;
   cudaStream_t s = nullptr;
+  cudaMemPool_t pool = nullptr;  // the tables' stream-ordered pool
   std::deque<hx::Pending> queue;
   std::vector<hx::Slot> slots;
   uint64_t seq = 0;
@@ -425,16 +426,21 @@ hx_status hx_server_create(hx_server** out, int key_bytes, uint64_t memory_budge
   sv->max_round_keys = max_round_keys;
   const uint64_t max_tiles = max_round_requests + max_round_keys / 256 + 1;
   cudaError_t e = cudaStreamCreateWithFlags(&sv->s, cudaStreamNonBlocking);
-  // Tables grow and shrink through the stream-ordered allocator: keep freed
-  // memory in the device's default pool instead of returning it to the
-  // driver at every synchronisation (a process-local pool attribute).
+  // Tables grow and shrink through the stream-ordered allocator, from a pool
+  // of the server's own: freed tables stay in it (release threshold = max)
+  // instead of going back to the driver at every synchronisation, and no
+  // other allocation of the process (torch's, another library's) is affected.
   {
     int dev = 0;
-    cudaMemPool_t pool;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetDefaultMemPool(&pool, dev);
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    if (e == cudaSuccess) e = cudaMemPoolCreate(&sv->pool, &props);
     uint64_t keep = ~0ull;
-    if (e == cudaSuccess) e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (e == cudaSuccess) e = cudaMemPoolSetAttribute(sv->pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&sv->d_maps), max_maps * sizeof(SMap));
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&sv->d_info), max_maps * sizeof(DInfo));
@@ -492,6 +498,10 @@ hx_status hx_server_destroy(hx_server* sv) {
   cudaFree(sv->d_info);
   if (sv->t0) cudaEventDestroy(sv->t0);
   if (sv->s) cudaStreamDestroy(sv->s);
+  if (sv->pool) {
+    cudaDeviceSynchronize();  // every table's free has completed
+    cudaMemPoolDestroy(sv->pool);
+  }
   delete sv;
   return HX_OK;
 }
@@ -504,7 +514,7 @@ hx_status hx_server_add_map(hx_server* sv, int size_power, uint32_t* map_id) {
   ServeMap m;
   m.sp = size_power;
   m.bytes = bytes;
-  HX_CUDA(cudaMallocAsync(&m.table, bytes, sv->s));
+  HX_CUDA(cudaMallocFromPoolAsync(&m.table, bytes, sv->pool, sv->s));
   hx_map v;
   v.key_bytes = sv->kb;
   v.val_bytes = sv->kb;
@@ -608,7 +618,7 @@ static hx_status server_step(hx_server* sv, uint32_t* launched) {
       // replaces the pending target with the larger table
       int& slot_of = grow_of[r.map];
       void* nt = nullptr;
-      HX_CUDA(cudaMallocAsync(&nt, nbytes, sv->s));
+      HX_CUDA(cudaMallocFromPoolAsync(&nt, nbytes, sv->pool, sv->s));
       if (slot_of < 0) {
         slot_of = (int)tasks.size();
         tasks.push_back(GrowTask{m.table, nt, 1ull << m.sp, nsp, r.map});

@@ -256,6 +256,23 @@ def affine_sample(n: int, k: int, rng) -> np.ndarray:
     return (a * j + b) % n
 
 
+def query_expectation(keys: np.ndarray, vals: np.ndarray, q: np.ndarray, fill: int):
+    """Exact retrieve output for a map holding the distinct keys `keys` with
+    `vals`: the value of each query key that is present, `fill` (the output's
+    pre-fill, which a miss leaves in place) for the others. Returns (expected
+    output, found mask)."""
+    out = np.full(len(q), fill, keys.dtype)
+    if len(keys) == 0 or len(q) == 0:
+        return out, np.zeros(len(q), bool)
+    order = np.argsort(keys, kind="stable")
+    sk = keys[order]
+    pos = np.searchsorted(sk, q)
+    pos[pos == len(sk)] = 0
+    found = sk[pos] == q
+    out[found] = vals[order[pos[found]]]
+    return out, found
+
+
 def large_map_workload(n: int, width: int, seed: int, hit_frac: float = 0.5, erase_frac: float = 0.3):
     """map_workload for very large n without O(n log n) sampling: hits and the
     erase set are affine samples of the inserted keys, the query order an

@@ -46,7 +46,9 @@ enum { HX_STATUS_SUCCESS = 0, HX_STATUS_FAIL = 1, HX_STATUS_INVALID = 2 };
  * (hashinator/defaults.h:44-54). current_max_bucket_overflow keeps the
  * reference's meaning (the probe bound rounded up to a multiple of 32,
  * never below 32, common.h:54-57); max_probe is the exact longest probe
- * (distance + 1) that the device kernels use as their search bound. */
+ * (distance + 1) that the device kernels use as their search bound.
+ * last_clean_moved has no reference counterpart; it sizes the moved-key term
+ * of clean_tombstones' traffic. */
 typedef struct hx_info {
   int32_t size_power;
   int32_t err;
@@ -55,6 +57,8 @@ typedef struct hx_info {
   uint64_t tombstone_counter;
   uint64_t max_probe;
   uint64_t bucket_count;
+  uint64_t last_clean_moved; /* keys the last clean_tombstones took out and
+                                inserted again (0 when it found no tombstones) */
 } hx_info;
 
 /* Predicate descriptor: the C-ABI stand-in for the reference's `Rule`
@@ -338,11 +342,11 @@ hx_status hx_batch_inject_stall(hx_batch_plan* plan, uint32_t map, int phase, in
  * whose load factor would pass max_load_factor is grown by an on-device
  * rehash; tables are admitted against memory_budget_bytes, and an insert
  * that cannot grow its table within the budget completes with HX_ERR_OOM.
- * One host thread drives a server. Tables live in the device's default
- * stream-ordered memory pool, and hx_server_create sets that pool's release
- * threshold to keep freed memory (cudaMemPoolAttrReleaseThreshold = max), so
- * that growth does not return memory to the driver at every synchronisation;
- * the setting belongs to the process and stays after hx_server_destroy. */
+ * One host thread drives a server. Tables live in a stream-ordered memory
+ * pool that the server creates for itself, with its release threshold at
+ * the maximum, so that growth does not return memory to the driver at every
+ * synchronisation; the process's other pools are left as they were, and
+ * hx_server_destroy destroys the server's pool (it synchronises the device). */
 typedef struct hx_server hx_server;
 enum { HX_OP_INSERT = 0, HX_OP_QUERY = 1, HX_OP_ERASE = 2 };
 typedef struct hx_request {
@@ -405,9 +409,16 @@ hx_status hx_server_run_trace(hx_server* server, const hx_request* requests, con
  *   and launches nothing. In-place (d_out == d_in) is allowed.
  * - The first call on each device looks up the array's device address (with
  *   that device current); make that first call before any stream capture.
+ *   The address is kept for the device's current context; after a
+ *   cudaDeviceReset the next call looks it up again in the new context.
  * - Every call shares the one array and clears the part it uses. Calls that
  *   overlap on the GPU race on it and give wrong results: serialise them,
  *   for example on one stream.
+ * - The scan's waits between tiles are bounded. If one runs out (which
+ *   needs the GPU to stop scheduling the kernel's blocks), this entry point
+ *   cannot report it: it returns before the kernel ends, and the array that
+ *   would hold the error word is private and cleared by the next call. The
+ *   allocating scan with caller scratch reports HX_ERR_TIMEOUT instead.
  * - No cudaMalloc, cudaFree or allocating library call is made. */
 #define HX_NOALLOC_SCAN_MAX_N (1ull << 28)
 #define HX_NOALLOC_SCAN_SCRATCH_BYTES (256ull + 8ull * (HX_NOALLOC_SCAN_MAX_N / 4096ull))

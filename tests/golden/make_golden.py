@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
 Runs the reference Hashinator in its own CPU-only mode (oracle/_ref/ref_driver,
-built by `make -C oracle` from the reference source tree) on seeded inputs
+built by oracle/build_ref.sh from the reference source tree) on seeded inputs
 from hashinator_gb300.workloads and stores inputs and outputs as compressed
 .npz files. Needs the reference source tree (only present where the fixtures
 are made); the fixtures themselves are committed and read by the tests.
@@ -114,7 +114,7 @@ def make_duplicates() -> None:
 
 if __name__ == "__main__":
     if not DRIVER.exists():
-        sys.exit(f"{DRIVER} missing: run `make -C oracle` where the reference source tree is present")
+        sys.exit(f"{DRIVER} missing: run oracle/build_ref.sh where the reference source tree is present")
     if "--extra" not in sys.argv[1:]:
         for nm, args in CASES.items():
             make_case(nm, *args)

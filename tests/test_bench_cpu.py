@@ -13,8 +13,9 @@ def test_reference_arm_json_line():
     sys.path.insert(0, str(ROOT))
     import bench
 
+    # a 2^22-key headline (the default is 2^26; the arm runs whatever size it is given, in full)
     r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "3"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+                        "--warmup", "3", "--log-keys", "22"], cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
     assert len(lines) == 1
@@ -23,11 +24,11 @@ def test_reference_arm_json_line():
               "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert k in d, k
     assert d["impl"] == "reference" and d["n_gpus"] == 1 and d["steps"] == 1 and d["warmup"] == 3
-    assert d["metric"] == bench.headline_metric(26) and d["unit"] == "Mkeys/s" and d["higher_is_better"] is True
+    assert d["metric"] == bench.headline_metric(22) and d["unit"] == "Mkeys/s" and d["higher_is_better"] is True
     assert d["value"] > 0 and d["ms_per_step"] > 0
     cfg = dict(d["config"])
-    assert cfg.pop("reference_host_threads") >= 1 and cfg.pop("reference_sample")
-    assert cfg == bench.headline_config(26, 0)
+    assert cfg.pop("reference_host_threads") >= 1 and cfg.pop("reference_sample").endswith("(the full workload)")
+    assert cfg == bench.headline_config(22, 0)
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["value"] == d["value"] and cb["unit"] == d["unit"] and cb["cores"] >= 1
     assert cb["sample"]
@@ -114,7 +115,7 @@ def test_reference_arm_under_two_ranks():
     env = dict(os.environ, OMP_NUM_THREADS="1")
     r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
                         "--master-addr", "127.0.0.1", "--master-port", str(port), str(ROOT / "bench.py"),
-                        "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3"],
+                        "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3", "--log-keys", "20"],
                        cwd=ROOT, capture_output=True, text=True, timeout=900, env=env)
     assert r.returncode == 0, r.stderr[-3000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
