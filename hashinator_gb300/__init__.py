@@ -25,7 +25,7 @@ import os
 from pathlib import Path
 
 __all__ = ["lib", "HXError", "Hashmap", "Pred", "tools", "Batch", "BatchPlan", "Server", "Request", "Completion",
-           "STATUS_SUCCESS", "STATUS_FAIL", "STATUS_INVALID", "LIB_PATH", "Info"]
+           "STATUS_SUCCESS", "STATUS_FAIL", "STATUS_INVALID", "LIB_PATH", "Info", "BatchTrial"]
 
 LIB_PATH = Path(__file__).resolve().parent / "libhx.so"
 
@@ -150,6 +150,10 @@ _SIGS.update({
     "hx_batch_set_tuning": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
     "hx_batch_run": [ctypes.c_void_p, ctypes.c_void_p],
     "hx_batch_run_graph": [ctypes.c_void_p, ctypes.c_void_p],
+    "hx_batch_autotune": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_uint32,
+                          ctypes.POINTER(ctypes.c_int32), ctypes.c_uint32, ctypes.POINTER(ctypes.c_int32),
+                          ctypes.c_uint32, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                          ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p],
     "hx_batch_run_per_map": [ctypes.c_void_p, ctypes.c_void_p],
     "hx_batch_check": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p],
     "hx_batch_inject_stall": [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
@@ -526,6 +530,16 @@ class Batch:
                          erase_offsets, clean, stream)
 
 
+class BatchTrial(ctypes.Structure):
+    """hx_batch_trial: one point of the autotuner's grid and its time."""
+    _fields_ = [("group_width", ctypes.c_int32), ("block_size", ctypes.c_int32), ("tile_keys", ctypes.c_int32),
+                ("ms", ctypes.c_float)]
+
+
+# hx_batch_reset_fn: hx_status (*)(void* user, hx_stream stream)
+BATCH_RESET_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p)
+
+
 class BatchPlan:
     """One round of work over a Batch, run as one persistent launch."""
 
@@ -570,6 +584,39 @@ class BatchPlan:
 
     def run_per_map(self, stream=None) -> None:
         _check(self._h.hx_batch_run_per_map(self._p, _stream(stream)), "hx_batch_run_per_map")
+
+    def autotune(self, groups=None, blocks=None, tiles=None, reps: int = 2, reset=None, stream=None):
+        """hx_batch_autotune: times the captured-graph replay over the grid (None: libhx's default grid)
+        and leaves the plan on the fastest point. reset: None (the maps are cleared before every trial) or
+        a callable(stream) that restores the state the round starts from. Returns (best, trials) with
+        best = (group, block, tile, ms)."""
+        def arr(v):
+            if v is None:
+                return None, 0
+            a = (ctypes.c_int32 * len(v))(*v)
+            return a, len(v)
+
+        g, ng = arr(groups)
+        b, nb = arr(blocks)
+        t, nt = arr(tiles)
+        n = (ng or 5) * (nb or 3) * (nt or 3)
+        trials = (BatchTrial * n)()
+        best = BatchTrial()
+        cb = None
+        if reset is not None:
+            def _reset(user, strm):
+                try:
+                    reset(stream)
+                    return HX_OK
+                except Exception:  # noqa: BLE001
+                    return HX_ERR_INVALID_ARG
+            cb = BATCH_RESET_FN(_reset)
+        _check(self._h.hx_batch_autotune(self._p, g, ng, b, nb, t, nt, reps,
+                                         ctypes.cast(cb, ctypes.c_void_p) if cb else None, None, _stream(stream),
+                                         ctypes.byref(trials), n, ctypes.byref(best)), "hx_batch_autotune")
+        self.tuning = {"group_width": best.group_width, "block_size": best.block_size, "tile_keys": best.tile_keys}
+        return ((best.group_width, best.block_size, best.tile_keys, best.ms),
+                [(x.group_width, x.block_size, x.tile_keys, x.ms) for x in trials])
 
     def inject_stall(self, map_index: int, phase: int, enable: bool = True, stream=None) -> None:
         """Test hook: make the later phases of one map wait for a tile that never runs."""

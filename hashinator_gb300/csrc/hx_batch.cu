@@ -18,6 +18,7 @@
 #include <cstring>
 #include <vector>
 
+#include "hx_autotune.h"
 #include "hx_host.h"
 #include "hx_internal.h"
 #include "hx_probe.cuh"
@@ -763,6 +764,73 @@ hx_status hx_batch_run_graph(hx_batch_plan* p, hx_stream stream) {
   }
   account_inserts(p);
   HX_CUDA(cudaGraphLaunch(p->graph_exec, s));
+  return HX_OK;
+}
+
+hx_status hx_batch_autotune(hx_batch_plan* p, const int32_t* group_widths, uint32_t n_groups,
+                            const int32_t* block_sizes, uint32_t n_blocks, const int32_t* tile_keys, uint32_t n_tiles,
+                            int reps, hx_batch_reset_fn reset, void* reset_user, hx_stream stream,
+                            hx_batch_trial* trials, uint32_t trials_capacity, hx_batch_trial* best) {
+  HX_RANGE("hx_batch_autotune");
+  if (!p || !best || reps < 1) return HX_ERR_INVALID_ARG;
+  static const int32_t kGroups[] = {1, 4, 8, 16, 32}, kBlocks[] = {128, 256, 512}, kTiles[] = {512, 2048, 8192};
+  if (!group_widths) {
+    group_widths = kGroups;
+    n_groups = 5;
+  }
+  if (!block_sizes) {
+    block_sizes = kBlocks;
+    n_blocks = 3;
+  }
+  if (!tile_keys) {
+    tile_keys = kTiles;
+    n_tiles = 3;
+  }
+  if (!n_groups || !n_blocks || !n_tiles) return HX_ERR_INVALID_ARG;
+  std::vector<TunePoint> grid;
+  for (uint32_t g = 0; g < n_groups; ++g)
+    for (uint32_t b = 0; b < n_blocks; ++b)
+      for (uint32_t t = 0; t < n_tiles; ++t) grid.push_back(TunePoint{group_widths[g], block_sizes[b], tile_keys[t]});
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  HX_CUDA(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return cuda_status(cudaGetLastError());
+  }
+  // One trial = one replay of the plan's captured graph (the launch the
+  // product runs), timed with events on the caller's stream.
+  struct Runner {
+    hx_batch_plan* p;
+    hx_batch_reset_fn reset_fn;
+    void* user;
+    hx_stream stream;
+    cudaStream_t s;
+    cudaEvent_t e0, e1;
+    hx_status set(const TunePoint& t) { return hx_batch_set_tuning(p, t.group, t.block, t.tile, stream); }
+    hx_status reset() { return reset_fn ? reset_fn(user, stream) : hx_batch_clear(p->b, stream); }
+    hx_status timed_run(float* ms) {
+      HX_CUDA(cudaEventRecord(e0, s));
+      hx_status st = hx_batch_run_graph(p, stream);
+      if (st != HX_OK) return st;
+      HX_CUDA(cudaEventRecord(e1, s));
+      HX_CUDA(cudaEventSynchronize(e1));
+      HX_CUDA(cudaEventElapsedTime(ms, e0, e1));
+      int32_t err = 0;
+      if ((st = hx_batch_check(p, &err, stream)) != HX_OK) return st;
+      return err == 1 ? HX_ERR_TIMEOUT : (err == 2 ? HX_ERR_CAPACITY : HX_OK);
+    }
+  } runner{p, reset, reset_user, stream, s, e0, e1};
+  std::vector<float> ms(grid.size(), 0.f);
+  TunePoint bp{};
+  float bms = 0.f;
+  const hx_status st = autotune_grid(runner, grid.data(), grid.size(), reps, ms.data(), &bp, &bms);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != HX_OK) return st;
+  for (size_t i = 0; i < grid.size() && trials && i < trials_capacity; ++i)
+    trials[i] = hx_batch_trial{grid[i].group, grid[i].block, grid[i].tile, ms[i]};
+  *best = hx_batch_trial{bp.group, bp.block, bp.tile, bms};
   return HX_OK;
 }
 

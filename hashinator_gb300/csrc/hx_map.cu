@@ -751,24 +751,25 @@ static hx_status extract(hx_map* m, const hx_pred* pred, void* d_out, uint64_t c
   std::lock_guard<std::mutex> g(m->mu);
   const uint64_t n = nslots(m);
   const bool p32 = is_p32(m);
-  const uint64_t tiles = p32 ? compact_tiles<P32>(n) : compact_tiles<P64>(n);
-  const uint64_t sc_bytes = (scan_scratch_bytes(tiles) + 255) / 256 * 256;
+  const uint64_t need = p32 ? compact_scratch_need<P32>(n) : compact_scratch_need<P64>(n);
+  const uint64_t sc_bytes = (need + 255) / 256 * 256;
   hx_status st = ensure_scratch(m, sc_bytes + 256, s);
   if (st != HX_OK) return st;
   unsigned long long* cnt = d_count ? reinterpret_cast<unsigned long long*>(d_count)
                                     : reinterpret_cast<unsigned long long*>(static_cast<char*>(m->scratch) + sc_bytes);
   cudaError_t e;
   CleanArgs cl{nullptr, nullptr};
+  bool sk = false;
   if (p32) {
     using O = typename std::conditional<KEYS, uint32_t, P32>::type;
     e = launch_compact<P32, false, O>(static_cast<const P32*>(m->buckets), static_cast<O*>(d_out), n, *pred,
                                       TableRef<P32>{static_cast<const P32*>(m->buckets), m->sp}, capacity, cnt,
-                                      m->scratch, cl, s);
+                                      m->scratch, cl, s, &sk);
   } else {
     using O = typename std::conditional<KEYS, uint64_t, P64>::type;
     e = launch_compact<P64, false, O>(static_cast<const P64*>(m->buckets), static_cast<O*>(d_out), n, *pred,
                                       TableRef<P64>{static_cast<const P64*>(m->buckets), m->sp}, capacity, cnt,
-                                      m->scratch, cl, s);
+                                      m->scratch, cl, s, &sk);
   }
   if (e != cudaSuccess) return cuda_status(e);
   if ((st = after_launch()) != HX_OK) return st;
@@ -776,7 +777,7 @@ static hx_status extract(hx_map* m, const hx_pred* pred, void* d_out, uint64_t c
     unsigned long long c = 0;
     unsigned int err = 0;
     HX_CUDA(cudaMemcpyAsync(&c, cnt, sizeof(c), cudaMemcpyDeviceToHost, s));
-    HX_CUDA(cudaMemcpyAsync(&err, static_cast<char*>(m->scratch) + 4, sizeof(err), cudaMemcpyDeviceToHost, s));
+    HX_CUDA(cudaMemcpyAsync(&err, scan_error_word(m->scratch, sk), sizeof(err), cudaMemcpyDeviceToHost, s));
     HX_CUDA(cudaStreamSynchronize(s));
     *h_count = c;
     if (err) return HX_ERR_TIMEOUT;
@@ -915,8 +916,8 @@ hx_status hx_clean_tombstones(hx_map* m, hx_stream stream) {
   std::lock_guard<std::mutex> g(m->mu);
   const uint64_t n = nslots(m);
   const bool p32 = is_p32(m);
-  const uint64_t tiles = p32 ? compact_tiles<P32>(n) : compact_tiles<P64>(n);
-  const uint64_t sc_bytes = (scan_scratch_bytes(tiles) + 255) / 256 * 256;
+  const uint64_t need = p32 ? compact_scratch_need<P32>(n) : compact_scratch_need<P64>(n);
+  const uint64_t sc_bytes = (need + 255) / 256 * 256;
   const uint64_t cap = m->fill_ub < n ? m->fill_ub : n;  // moved keys <= fill <= fill_ub
   hx_status st = ensure_scratch(m, sc_bytes + (cap + 1) * pair_bytes(m), s);
   if (st != HX_OK) return st;

@@ -21,13 +21,16 @@
 
 namespace hx {
 
-constexpr uint64_t kNoAllocTileElems = (uint64_t)kScanBlock * kScanTmaR * 4;  // the smaller scan tiles
+// Both scan kernels fit the array at the largest n: the register-staged one
+// (one status word per tile of 12288 elements) and the phase-partitioned one
+// (count slots for its largest grid).
+constexpr uint64_t kNoAllocTileElems = (uint64_t)kScanBlock * kScanR * 4;
 constexpr uint64_t kNoAllocTiles = (HX_NOALLOC_SCAN_MAX_N + kNoAllocTileElems - 1) / kNoAllocTileElems;
 static_assert(256 + 8 * kNoAllocTiles <= HX_NOALLOC_SCAN_SCRATCH_BYTES, "ticket/error words + tile statuses fit");
+static_assert(hxs::kScratchBytes <= HX_NOALLOC_SCAN_SCRATCH_BYTES, "error word + count slots fit");
 
-// Look-back scratch of the no-allocation scan: 256 B of ticket and error
-// words, then one 8-byte status word per tile of 4096 elements (524,544 B for
-// the largest scan, 2^28 elements).
+// Scratch of the no-allocation scan, HX_NOALLOC_SCAN_SCRATCH_BYTES
+// (524,544 B): room for either scan kernel's words at n = 2^28.
 static __device__ __align__(256) unsigned char g_noalloc_scan_scratch[HX_NOALLOC_SCAN_SCRATCH_BYTES];
 
 // The current context's driver-assigned id (unique for the life of the
@@ -105,9 +108,7 @@ extern "C" hx_status hx_exclusive_scan_u32_noalloc(const uint32_t* d_in, uint32_
   cudaError_t e;
   void* sc = noalloc_scratch(dev, &e);
   if (!sc) return cuda_status(e);
-  const uint64_t tiles = scan_tiles(n);
-  // The previous call left its tickets and statuses behind: reset the part used.
-  HX_CUDA(cudaMemsetAsync(sc, 0, scan_scratch_bytes(tiles), s));
+  // The previous call left its words behind: launch_scan resets the part it uses.
   HX_CUDA(launch_scan(d_in, d_out, n, sc, s));
   return after_launch();
 }

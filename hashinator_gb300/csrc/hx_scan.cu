@@ -72,7 +72,7 @@ static hx_status finish_sync(cudaStream_t s, const unsigned long long* d_count, 
 // for a device count word when the caller gives none.
 template <class T>
 static uint64_t compact_scratch_bytes(uint64_t n) {
-  return scan_scratch_bytes(compact_tiles<T>(n)) + 256;
+  return (compact_scratch_need<T>(n) + 255) / 256 * 256 + 256;
 }
 
 template <class T>
@@ -85,18 +85,19 @@ static hx_status copy_if_t(const void* d_in, void* d_out, uint64_t n, const hx_p
   if (st != HX_OK) return st;
   unsigned long long* cnt = d_count ? reinterpret_cast<unsigned long long*>(d_count)
                                     : reinterpret_cast<unsigned long long*>(static_cast<char*>(sc.ptr) + need - 256);
+  bool sk = false;
   if (n == 0) {
     HX_CUDA(cudaMemsetAsync(cnt, 0, sizeof(*cnt), s));
     HX_CUDA(cudaMemsetAsync(sc.ptr, 0, 256, s));
   } else {
     typename ElemOps<T>::Ctx ctx{};
     cudaError_t e = launch_compact<T, false>(static_cast<const T*>(d_in), static_cast<T*>(d_out), n, pr, ctx,
-                                             capacity, cnt, sc.ptr, CleanArgs{nullptr, nullptr}, s);
+                                             capacity, cnt, sc.ptr, CleanArgs{nullptr, nullptr}, s, &sk);
     if (e != cudaSuccess) return cuda_status(e);
     st = after_launch();
     if (st != HX_OK) return st;
   }
-  if (h_count) return finish_sync(s, cnt, h_count, reinterpret_cast<unsigned int*>(sc.ptr) + 1, capacity);
+  if (h_count) return finish_sync(s, cnt, h_count, scan_error_word(sc.ptr, sk), capacity);
   return HX_OK;
 }
 
@@ -187,7 +188,7 @@ hx_status hx_diag_random_access(void* d_buf, uint64_t bytes, uint64_t n_ops, int
 hx_status hx_scratch_bytes(int op, uint64_t n, uint64_t* bytes) {
   if (!bytes) return HX_ERR_INVALID_ARG;
   if (op == HX_SCRATCH_SCAN) {
-    *bytes = scan_scratch_bytes(scan_tiles(n));
+    *bytes = scan_scratch_need(n);
   } else if (op == HX_SCRATCH_COPY_IF) {
     // the largest of the three element widths' needs
     uint64_t a = compact_scratch_bytes<uint32_t>(n), b = compact_scratch_bytes<P32>(n),
@@ -208,9 +209,8 @@ hx_status hx_exclusive_scan_u32(const uint32_t* d_in, uint32_t* d_out, uint64_t 
   const uint64_t tiles = scan_tiles(n);
   if (tiles > 0xFFFFFFFFull) return HX_ERR_INVALID_ARG;
   Scratch sc;
-  hx_status st = sc.get(d_scratch, scratch_bytes, scan_scratch_bytes(tiles), s);
+  hx_status st = sc.get(d_scratch, scratch_bytes, scan_scratch_need(n), s);
   if (st != HX_OK) return st;
-  HX_CUDA(cudaMemsetAsync(sc.ptr, 0, scan_scratch_bytes(tiles), s));
   HX_CUDA(launch_scan(d_in, d_out, n, sc.ptr, s));
   return after_launch();
 }

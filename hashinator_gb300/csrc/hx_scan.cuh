@@ -17,6 +17,7 @@
 // host turns that word into HX_ERR_TIMEOUT.
 #pragma once
 #include "hx_device.cuh"
+#include "../../include/hx_stream.cuh"
 #include <mutex>
 #include <set>
 #include <atomic>
@@ -216,191 +217,6 @@ __global__ void __launch_bounds__(BLOCK) k_scan_u32(const uint32_t* in, uint32_t
       for (int q = 0; q < 4; ++q)
         if (e + q < n) out[e + q] = o[q];
     }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Exclusive u32 scan with TMA staging (the path for 16-byte-aligned buffers).
-// Tiles of BLOCK*R uint4 are copied into shared memory by one bulk copy each
-// (cp.async.bulk, completion on an mbarrier), two stages per CTA: while the
-// CTA looks back and writes tile k, tile k+1 is already loaded and its
-// aggregate published, and tile k+2 is in flight. Publishing every aggregate
-// an iteration before its own look-back shortens the waits of later tiles.
-// Persistent CTAs take tickets in order and finish their tiles in order; a
-// tile's aggregate depends only on its CTA's own copy and on look-backs of
-// lower tiles, so the lowest unpublished tile can always progress. Every wait
-// is bounded: an mbarrier wait gives up after about a second; the CTA then
-// stops taking tiles at the end of that iteration, waits once more (bounded)
-// for each bulk copy it issued that has not completed, records the error and
-// returns. Tiles it never published are resolved by the bounded look-back of
-// later tiles, which record the error too.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
-  if (mbar_try_wait(bar, parity)) return true;
-  unsigned long long t0;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
-  for (unsigned i = 0; i < (1u << 26); ++i) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((i & 255) == 255) {
-      unsigned long long t;
-      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-      if (t - t0 > 1000000000ull) return false;
-    }
-  }
-  return false;
-}
-// One bulk copy global -> shared of `bytes` (multiple of 16, both addresses
-// 16-byte aligned), completing `bytes` transactions on `bar`.
-__device__ __forceinline__ void bulk_load(void* dst_smem, const void* src, unsigned bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_addr(dst_smem)),
-               "l"(src), "r"(bytes), "r"(smem_addr(bar))
-               : "memory");
-}
-
-template <int BLOCK, int R>
-__global__ void __launch_bounds__(BLOCK) k_scan_u32_tma(const uint32_t* in, uint32_t* out, uint64_t n,
-                                                       ScanScratch sc) {
-  constexpr int WARPS = BLOCK / 32;
-  constexpr unsigned TILE = BLOCK * R * 4;  // u32 per tile
-  constexpr unsigned TBYTES = TILE * 4;
-  extern __shared__ __align__(128) uint4 s_buf[];  // 2 stages of TILE / 4 uint4
-  __shared__ __align__(8) uint64_t s_bar[2];
-  __shared__ unsigned long long s_tile[2];
-  __shared__ unsigned s_wtot[2][WARPS];
-  __shared__ unsigned long long s_prefix;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const unsigned long long tiles = (n + TILE - 1) / TILE;
-  const unsigned long long full_tiles = n / TILE;
-  // Per stage s, bit s of: par = parity of the next wait on its barrier;
-  // pend = a fill was issued that this thread has not yet seen complete.
-  unsigned par = 0, pend = 0;
-  // Fill stage st with tile t: a full tile by one bulk copy, the ragged last
-  // tile by plain loads (zero beyond n). Called by all threads.
-  auto fill = [&](int st, unsigned long long t) {
-    uint4* dst = s_buf + (size_t)st * (TILE / 4);
-    if (t < full_tiles) {
-      if (threadIdx.x == 0) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier reads of the stage come first
-        mbar_arrive_expect_tx(&s_bar[st], TBYTES);
-        bulk_load(dst, in + t * TILE, TBYTES, &s_bar[st]);
-      }
-    } else {
-      const uint64_t base = t * TILE;
-      uint32_t* d = reinterpret_cast<uint32_t*>(dst);
-      for (unsigned i = threadIdx.x; i < TILE; i += BLOCK) d[i] = base + i < n ? in[base + i] : 0u;
-      __syncthreads();
-      if (threadIdx.x == 0) mbar_arrive_expect_tx(&s_bar[st], 0);
-    }
-    pend |= 1u << st;
-  };
-  if (threadIdx.x == 0) {
-    mbar_init(&s_bar[0], 1);
-    mbar_init(&s_bar[1], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    s_tile[0] = atomicAdd(sc.ticket, 1u);
-    s_tile[1] = atomicAdd(sc.ticket, 1u);
-  }
-  __syncthreads();
-  unsigned long long cur = s_tile[0], nxt = s_tile[1];
-  if (cur >= tiles) return;
-  fill(0, cur);
-  if (nxt < tiles) fill(1, nxt);
-  bool ok = true, failed = false;
-  // Per-warp totals of the tile in stage st, and its aggregate published.
-  auto reduce = [&](int st, unsigned long long t) {
-    if (ok) {
-      ok = mbar_wait_bounded(&s_bar[st], (par >> st) & 1u);
-      if (ok) {
-        par ^= 1u << st;
-        pend &= ~(1u << st);
-      }
-    }
-    const uint4* b = s_buf + (size_t)st * (TILE / 4) + warp * 32 * R;
-    unsigned acc = 0;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const uint4 q = b[r * 32 + lane];
-      acc += q.x + q.y + q.z + q.w;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) s_wtot[st][warp] = acc;
-    __syncthreads();
-    if (warp == 0 && t > 0) {
-      unsigned tot = lane < WARPS ? s_wtot[st][lane] : 0u;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
-      if (lane == 0) st_status(sc.status + t, kStAgg | (tot & kStVal));
-    }
-  };
-  reduce(0, cur);
-  int st = 0;
-  while (true) {
-    if (nxt < tiles) reduce(st ^ 1, nxt);  // the next tile's aggregate first
-    if (warp == 0) {
-      unsigned tot = lane < WARPS ? s_wtot[st][lane] : 0u;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
-      const unsigned long long tp = lookback(sc, cur, tot, lane);
-      if (lane == 0) s_prefix = tp;
-    }
-    __syncthreads();
-    {
-      unsigned acc = (unsigned)s_prefix;
-      for (int w = 0; w < warp; ++w) acc += s_wtot[st][w];
-      const uint4* b = s_buf + (size_t)st * (TILE / 4) + warp * 32 * R;
-      const uint64_t chunk = cur * TILE + (uint64_t)warp * 32 * R * 4;
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const uint4 q = b[r * 32 + lane];
-        const unsigned sum = q.x + q.y + q.z + q.w;
-        const unsigned incl = warp_incl_scan(sum, lane);
-        const unsigned o0 = acc + incl - sum, o1 = o0 + q.x, o2 = o1 + q.y, o3 = o2 + q.z;
-        acc += __shfl_sync(0xffffffffu, incl, 31);
-        const uint64_t e = chunk + ((uint64_t)r * 32 + lane) * 4;
-        if (e + 4 <= n) {
-          __stcs(reinterpret_cast<uint4*>(out + e), make_uint4(o0, o1, o2, o3));
-        } else {
-          const unsigned o[4] = {o0, o1, o2, o3};
-#pragma unroll
-          for (int k = 0; k < 4; ++k)
-            if (e + k < n) out[e + k] = o[k];
-        }
-      }
-    }
-    failed = __syncthreads_or(!ok);  // stage st and its totals are free
-    if (failed || nxt >= tiles) break;
-    if (threadIdx.x == 0) s_tile[st] = atomicAdd(sc.ticket, 1u);
-    __syncthreads();
-    const unsigned long long after = s_tile[st];
-    if (after < tiles) fill(st, after);
-    cur = nxt;
-    nxt = after;
-    st ^= 1;
-  }
-  if (failed && threadIdx.x == 0) {
-    // No fill follows a failed wait, so each stage has at most one copy
-    // outstanding; give each one more bounded wait before the CTA exits.
-    for (int s = 0; s < 2; ++s)
-      if ((pend >> s) & 1u) mbar_wait_bounded(&s_bar[s], (par >> s) & 1u);
-    atomicExch(sc.error, 1u);
   }
 }
 
@@ -641,7 +457,6 @@ __global__ void __launch_bounds__(BLOCK) k_compact(const T* __restrict__ in, O* 
 // ---- host launch helpers ---------------------------------------------------
 constexpr int kScanBlock = 256;
 constexpr int kScanR = 12;     // register kernel: 256 threads x 12 uint4 = 12288 u32 per tile (sweep of 4..16)
-constexpr int kScanTmaR = 4;   // TMA kernel: 256 x 4 uint4 = 4096 u32 (16 KiB) per stage (sweep of 16-64 KiB)
 constexpr int kCompactBlock = 256;
 constexpr int kCompactR = 4;  // 256 threads x 4 uint4 = 16 KiB per sub-tile
 #ifndef HX_COMPACT_S
@@ -649,9 +464,10 @@ constexpr int kCompactR = 4;  // 256 threads x 4 uint4 = 16 KiB per sub-tile
 #endif
 constexpr int kCompactS = HX_COMPACT_S;  // sub-tiles per tile
 
-// Status words a scan of n elements may need: the TMA kernel's smaller tiles.
+// Tiles of the register-staged scan (the path for buffers that are not
+// 16-byte aligned).
 inline uint64_t scan_tiles(uint64_t n) {
-  const uint64_t t = (uint64_t)kScanBlock * kScanTmaR * 4;
+  const uint64_t t = (uint64_t)kScanBlock * kScanR * 4;
   return (n + t - 1) / t;
 }
 template <class T>
@@ -663,6 +479,18 @@ inline uint64_t compact_tiles(uint64_t n) {
   const uint64_t t = compact_tile_elems<T>();
   return (n + t - 1) / t;
 }
+// Scratch a scan or a compaction of n elements needs, whichever kernel runs:
+// the look-back statuses of the register-staged kernels, or the count slots
+// of the phase-partitioned kernels (hx_stream.cuh).
+inline uint64_t scan_scratch_need(uint64_t n) {
+  const uint64_t a = scan_scratch_bytes(scan_tiles(n)), b = hxs::scratch_need(n, 4);
+  return a > b ? a : b;
+}
+template <class T>
+inline uint64_t compact_scratch_need(uint64_t n) {
+  const uint64_t a = scan_scratch_bytes(compact_tiles<T>(n)), b = hxs::scratch_need(n, sizeof(T));
+  return a > b ? a : b;
+}
 inline ScanScratch carve_scratch(void* p, uint64_t tiles) {
   ScanScratch sc;
   sc.ticket = reinterpret_cast<unsigned int*>(p);
@@ -671,6 +499,11 @@ inline ScanScratch carve_scratch(void* p, uint64_t tiles) {
   (void)tiles;
   return sc;
 }
+// Where each kernel family keeps its error word in the scratch.
+inline unsigned* scan_error_word(void* scratch, bool stream_kernel) {
+  return stream_kernel ? hxs::carve(scratch).error : carve_scratch(scratch, 0).error;
+}
+inline bool aligned16(const void* p) { return ((uintptr_t)p % 16) == 0; }
 
 // Raise a kernel's dynamic shared-memory limit once (per kernel and device)
 // when it needs more than the default 48 KiB.
@@ -690,58 +523,92 @@ inline cudaError_t allow_dynamic_smem(Kern kern, size_t smem) {
   return e;
 }
 
-// Launch one exclusive scan (n > 0) on zeroed scratch of
-// scan_scratch_bytes(scan_tiles(n)) bytes: the TMA kernel (persistent, two
-// 16 KiB stages per CTA) when both buffers are 16-byte aligned, else the
-// register kernel over every tile.
-inline cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint64_t n, void* scratch, cudaStream_t s) {
-  if (((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0) {
-    auto kern = k_scan_u32_tma<kScanBlock, kScanTmaR>;
-    constexpr size_t smem = 2ull * kScanBlock * kScanTmaR * 16;
-    static std::atomic<int> blocks_per_sm[64];  // occupancy per device, 0 until first queried
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    int per_sm = dev < 64 ? blocks_per_sm[dev].load(std::memory_order_relaxed) : 0;
-    if (per_sm == 0) {
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kScanBlock, smem);
-      if (e != cudaSuccess) return e;
-      if (per_sm < 1) per_sm = 1;
-      if (dev < 64) blocks_per_sm[dev].store(per_sm, std::memory_order_relaxed);  // every writer stores the same
-    }
-    int sms = 0;
-    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    const uint64_t tiles = scan_tiles(n);
-    const uint64_t cap = (uint64_t)sms * per_sm;
-    const unsigned grid = (unsigned)(tiles < cap ? tiles : cap);
-    kern<<<grid, kScanBlock, smem, s>>>(in, out, n, carve_scratch(scratch, tiles));
-  } else {
-    const uint64_t t = (uint64_t)kScanBlock * kScanR * 4;
-    const uint64_t tiles = (n + t - 1) / t;
-    k_scan_u32<kScanBlock, kScanR><<<(unsigned)tiles, kScanBlock, 0, s>>>(in, out, n, carve_scratch(scratch, tiles),
-                                                                         false);
-  }
+// Launch one exclusive scan (n > 0) with scratch of scan_scratch_need(n)
+// bytes, which is zeroed here: the phase-partitioned kernel when both
+// buffers are 16-byte aligned, else the register kernel over every tile.
+// Returns through *stream_kernel which one ran (for its error word).
+inline cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint64_t n, void* scratch, cudaStream_t s,
+                               bool* stream_kernel = nullptr) {
+  const bool sk = aligned16(in) && aligned16(out);
+  if (stream_kernel) *stream_kernel = sk;
+  if (sk)
+    return hxs::launch<uint32_t, uint32_t, hxs::ScanSel, true>(in, out, n, hxs::ScanSel{}, 0,
+                                                                          hxs::Done{}, scratch, s);
+  const uint64_t tiles = scan_tiles(n);
+  cudaError_t e = cudaMemsetAsync(scratch, 0, scan_scratch_bytes(tiles), s);
+  if (e != cudaSuccess) return e;
+  k_scan_u32<kScanBlock, kScanR><<<(unsigned)tiles, kScanBlock, 0, s>>>(in, out, n, carve_scratch(scratch, tiles),
+                                                                       false);
   return cudaGetLastError();
 }
 
-// Launch one compaction pass (n > 0). The scratch must hold
-// scan_scratch_bytes(compact_tiles<T>(n)) bytes; it is zeroed here.
+// The predicate of a compaction for the phase-partitioned kernel: one
+// compiled predicate kind (PK_*), and in clean_tombstones mode (CLEAN) the
+// rewrite of every TOMBSTONE and every selected bucket to (EMPTY, 0) after
+// it has been read (see CleanArgs for why concurrent reads of home buckets
+// are safe).
+template <class T, int PK, bool CLEAN>
+struct PredSel {
+  hx_pred pr;
+  uint64_t magic;
+  typename ElemOps<T>::Ctx ctx;
+  static constexpr bool kRewrites = CLEAN;
+  __device__ __forceinline__ bool operator()(const T& x) const {
+    return ElemOps<T>::template pred<PK>(pr, x, ctx, magic);
+  }
+  __device__ __forceinline__ void rewrite(T* in, uint64_t i, const T& x, bool selected) const {
+    if constexpr (CLEAN) {
+      using Tr = PairTraits<T>;
+      if (selected || x.first == Tr::TOMB) {
+        T empty;
+        empty.first = Tr::EMPTY;
+        empty.second = 0;
+        in[i] = empty;
+      }
+    }
+  }
+};
+
+// Launch one compaction pass (n > 0) with scratch of compact_scratch_need<T>(n)
+// bytes, which is zeroed here: the phase-partitioned kernel when the input
+// is 16-byte aligned, else the look-back kernel k_compact.
 template <class T, bool CLEAN, class O = T>
 inline cudaError_t launch_compact(const T* in, O* out, uint64_t n, const hx_pred& pr,
                                   typename ElemOps<T>::Ctx ctx, uint64_t capacity, unsigned long long* d_count,
-                                  void* scratch, CleanArgs cl, cudaStream_t s) {
+                                  void* scratch, CleanArgs cl, cudaStream_t s, bool* stream_kernel = nullptr) {
+  const bool sk = aligned16(in);
+  if (stream_kernel) *stream_kernel = sk;
+  if (sk) {
+    const hxs::Done done{d_count, CLEAN ? cl.fill : nullptr, CLEAN ? cl.skip : nullptr};
+    auto go = [&](auto sel) -> cudaError_t {
+      return hxs::launch<T, O, decltype(sel), false>(in, out, n, sel, capacity, done, scratch, s);
+    };
+    if constexpr (CLEAN) {
+      return go(PredSel<T, PK_GENERIC, true>{pr, 0, ctx});
+    } else {
+      switch (pred_kind<T>(pr)) {
+        case PK_MOD_LT32:
+          return go(PredSel<T, PK_MOD_LT32, false>{pr, fastmod_magic((uint32_t)pr.a), ctx});
+        case PK_MASK_EQ:
+          return go(PredSel<T, PK_MASK_EQ, false>{pr, 0, ctx});
+        case PK_VALID:
+          if constexpr (!std::is_same<T, uint32_t>::value) return go(PredSel<T, PK_VALID, false>{pr, 0, ctx});
+          [[fallthrough]];
+        default:
+          return go(PredSel<T, PK_GENERIC, false>{pr, 0, ctx});
+      }
+    }
+  }
   const uint64_t tiles = compact_tiles<T>(n);
   cudaError_t e = cudaMemsetAsync(scratch, 0, scan_scratch_bytes(tiles), s);
   if (e != cudaSuccess) return e;
-  const bool vec = ((uintptr_t)in % 16) == 0;
   const size_t smem = (size_t)compact_tile_elems<T>() * sizeof(O);
   const ScanScratch sc = carve_scratch(scratch, tiles);
   const unsigned grid = (unsigned)tiles;
   auto launch = [&](auto kern, uint64_t magic) -> cudaError_t {
     cudaError_t err = allow_dynamic_smem(kern, smem);
     if (err != cudaSuccess) return err;
-    kern<<<grid, kCompactBlock, smem, s>>>(in, out, n, pr, magic, ctx, capacity, d_count, sc, vec, cl);
+    kern<<<grid, kCompactBlock, smem, s>>>(in, out, n, pr, magic, ctx, capacity, d_count, sc, false, cl);
     return cudaGetLastError();
   };
   if constexpr (CLEAN) {

@@ -24,16 +24,22 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <initializer_list>
+#include <iterator>
 #include <limits>
+#include <new>
+#include <stdexcept>
 #include <type_traits>
 #include <utility>
 #include <vector>
 
 #include "hx.h"
 #include "hx_device_api.cuh"
+#include "hx_stream.cuh"
 
 namespace hxcompat {
 inline void check(hx_status st, const char* what) {
@@ -49,6 +55,12 @@ inline void check_cuda(cudaError_t e, const char* what) {
     std::abort();
   }
 }
+// A valid key: neither EMPTY nor TOMBSTONE (the rule of the reference's
+// extractLoop / extractAllKeys); at namespace scope so kernels can take it.
+template <typename P, typename K, K EMPTY, K TOMB>
+struct ValidKeyRule {
+  __host__ __device__ bool operator()(const P& p) const { return p.first != EMPTY && p.first != TOMB; }
+};
 }  // namespace hxcompat
 
 namespace Hashinator {
@@ -82,103 +94,424 @@ struct Info {
 
 namespace split {
 
-/* Managed-memory vector (the reference's default allocator is
- * cudaMallocManaged, split_allocators.h:62-129), with the subset of the
- * SplitVector surface the accelerated API and its tests use. */
+/* split_unified_allocator<T> (splitvector/split_allocators.h:62-129): the
+ * reference's default allocator, managed memory. SplitVector below always
+ * keeps its elements, size and capacity in managed memory, so the allocator
+ * parameter only spells the reference's type. */
 template <typename T>
-class SplitVector {
-  T* d_ = nullptr;
-  size_t size_ = 0, cap_ = 0;
+struct split_unified_allocator {
+  using value_type = T;
+};
 
-  void reallocate(size_t cap) {
-    T* p = nullptr;
-    if (cap) hxcompat::check_cuda(cudaMallocManaged(&p, cap * sizeof(T)), "cudaMallocManaged");
-    if (d_) {
+/* SplitInfo (splitvec.h:43-46): what copyMetadata copies out. */
+typedef struct SplitVectorInfo {
+  size_t size;
+  size_t capacity;
+} SplitInfo;
+
+namespace detail {
+template <typename T>
+__global__ void k_fill(T* p, size_t n, T v) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
+}
+}  // namespace detail
+
+/* SplitVector<T> (splitvector/splitvec.h:83-1560). Elements, size and
+ * capacity live in managed memory, as in the reference, so that the host and
+ * device code share one vector: upload() gives kernels a device copy of the
+ * object, and device_push_back / device_resize / device_insert change the
+ * size that the host reads after a synchronisation. The observable rules
+ * follow the reference's, including its quirks:
+ *   - SplitVector() has no storage; reserve(n) on it allocates n elements and
+ *     sets the size to n (splitvec.h:850-856); otherwise reserve grows to
+ *     twice the request unless eco is set;
+ *   - device_push_back fills at most capacity - 1 elements (splitvec.h:1070-1078);
+ *   - the iterator's postfix ++ and -- return the neighbour without moving
+ *     the iterator (splitvec.h:1133-1136);
+ *   - device_insert(it, first, last) writes the range at `it` and grows the
+ *     size by its length without moving later elements (splitvec.h:1362-1384),
+ *     and device_insert(it, n, val) leaves the first index + n elements in
+ *     place and puts the n copies after them (splitvec.h:1432-1460);
+ * where the reference would assert or write past the allocation (a full
+ * vector, an index out of range), the device calls here do nothing and
+ * device_push_back returns false. */
+template <typename T, class Allocator = split_unified_allocator<T>>
+class SplitVector {
+  T* data_ = nullptr;
+  size_t* meta_ = nullptr;  // managed: meta_[0] = size, meta_[1] = capacity
+  SplitVector* d_vec_ = nullptr;
+
+  static void fill_range(T* p, size_t n) {
+    if (!n) return;
+    if constexpr (std::is_trivially_copyable<T>::value) {
+      const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 4096);
+      detail::k_fill<<<blocks, 256>>>(p, n, T());
+      hxcompat::check_cuda(cudaGetLastError(), "k_fill");
       hxcompat::check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
-      for (size_t i = 0; i < size_ && i < cap; ++i) p[i] = d_[i];
-      cudaFree(d_);
+    } else {
+      for (size_t i = 0; i < n; ++i) new (&p[i]) T();
     }
-    d_ = p;
-    cap_ = cap;
+  }
+  static T* alloc_elems(size_t n) {
+    T* p = nullptr;
+    if (n) hxcompat::check_cuda(cudaMallocManaged(&p, n * sizeof(T)), "cudaMallocManaged");
+    fill_range(p, n);
+    return p;
+  }
+  void alloc_meta() {
+    if (!meta_) {
+      hxcompat::check_cuda(cudaMallocManaged(&meta_, 2 * sizeof(size_t)), "cudaMallocManaged");
+      meta_[0] = meta_[1] = 0;
+    }
+  }
+  // _allocate(size) (splitvec.h:181): size = capacity = n, elements T().
+  void allocate(size_t n) {
+    alloc_meta();
+    data_ = alloc_elems(n);
+    meta_[0] = meta_[1] = n;
+  }
+  void copy_elems(T* dst, const T* src, size_t n) {
+    if (!n) return;
+    hxcompat::check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    if constexpr (std::is_trivially_copyable<T>::value) {
+      hxcompat::check_cuda(cudaMemcpy(dst, src, n * sizeof(T), cudaMemcpyDefault), "cudaMemcpy");
+    } else {
+      for (size_t i = 0; i < n; ++i) dst[i] = src[i];
+    }
+  }
+  void reallocate(size_t cap) {
+    T* p = alloc_elems(cap);
+    copy_elems(p, data_, std::min(size(), cap));
+    if (data_) cudaFree(data_);
+    data_ = p;
+    meta_[1] = cap;
   }
 
  public:
   using value_type = T;
-  using iterator = T*;
-  using const_iterator = const T*;
-  SplitVector() = default;
-  explicit SplitVector(size_t n) { resize(n); }
+
+  /* iterator (splitvec.h:1101-1162), postfix ++ / -- as in the reference. */
+  class iterator {
+    T* p_;
+
+   public:
+    using iterator_category = std::forward_iterator_tag;
+    using value_type = T;
+    using difference_type = int64_t;
+    using pointer = T*;
+    using reference = T&;
+    __host__ __device__ iterator(T* p = nullptr) : p_(p) {}
+    __host__ __device__ T* data() const { return p_; }
+    __host__ __device__ T* operator->() const { return p_; }
+    __host__ __device__ T& operator*() const { return *p_; }
+    __host__ __device__ bool operator==(const iterator& o) const { return p_ == o.p_; }
+    __host__ __device__ bool operator!=(const iterator& o) const { return p_ != o.p_; }
+    __host__ __device__ iterator& operator++() {
+      ++p_;
+      return *this;
+    }
+    __host__ __device__ iterator operator++(int) const { return iterator(p_ + 1); }
+    __host__ __device__ iterator& operator--() {
+      --p_;
+      return *this;
+    }
+    __host__ __device__ iterator operator--(int) const { return iterator(p_ - 1); }
+    __host__ __device__ iterator& operator+=(int64_t d) {
+      p_ += d;
+      return *this;
+    }
+    __host__ __device__ iterator& operator-=(int64_t d) {
+      p_ -= d;
+      return *this;
+    }
+    __host__ __device__ iterator operator+(int64_t d) const { return iterator(p_ + d); }
+    __host__ __device__ iterator operator-(int64_t d) const { return iterator(p_ - d); }
+  };
+  class const_iterator {
+    const T* p_;
+
+   public:
+    using iterator_category = std::forward_iterator_tag;
+    using value_type = T;
+    using difference_type = int64_t;
+    using pointer = const T*;
+    using reference = const T&;
+    __host__ __device__ const_iterator(const T* p = nullptr) : p_(p) {}
+    __host__ __device__ const_iterator(const iterator& it) : p_(it.data()) {}
+    __host__ __device__ const T* data() const { return p_; }
+    __host__ __device__ const T* operator->() const { return p_; }
+    __host__ __device__ const T& operator*() const { return *p_; }
+    __host__ __device__ bool operator==(const const_iterator& o) const { return p_ == o.p_; }
+    __host__ __device__ bool operator!=(const const_iterator& o) const { return p_ != o.p_; }
+    __host__ __device__ const_iterator& operator++() {
+      ++p_;
+      return *this;
+    }
+    __host__ __device__ const_iterator operator++(int) const { return const_iterator(p_ + 1); }
+    __host__ __device__ const_iterator& operator--() {
+      --p_;
+      return *this;
+    }
+    __host__ __device__ const_iterator operator--(int) const { return const_iterator(p_ - 1); }
+    __host__ __device__ const_iterator operator+(int64_t d) const { return const_iterator(p_ + d); }
+    __host__ __device__ const_iterator operator-(int64_t d) const { return const_iterator(p_ - d); }
+  };
+
+  // ---- construction (splitvec.h:200-300) ----
+  SplitVector() { alloc_meta(); }
+  explicit SplitVector(size_t n) { allocate(n); }
   SplitVector(size_t n, const T& v) {
-    resize(n);
-    for (size_t i = 0; i < n; ++i) d_[i] = v;
+    allocate(n);
+    for (size_t i = 0; i < n; ++i) data_[i] = v;
+  }
+  SplitVector(std::initializer_list<T> init) {
+    allocate(init.size());
+    size_t i = 0;
+    for (const T& v : init) data_[i++] = v;
+  }
+  explicit SplitVector(const std::vector<T>& v) {
+    allocate(v.size());
+    for (size_t i = 0; i < v.size(); ++i) data_[i] = v[i];
   }
   SplitVector(const SplitVector& o) {
-    reserve(o.size_);
-    hxcompat::check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
-    for (size_t i = 0; i < o.size_; ++i) d_[i] = o.d_[i];
-    size_ = o.size_;
+    allocate(o.size());
+    copy_elems(data_, o.data_, o.size());
+  }
+  SplitVector(SplitVector&& o) noexcept : data_(o.data_), meta_(o.meta_) {
+    o.data_ = nullptr;
+    o.meta_ = nullptr;
   }
   SplitVector& operator=(const SplitVector& o) {
     if (this != &o) {
-      resize(o.size_);
-      hxcompat::check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
-      for (size_t i = 0; i < o.size_; ++i) d_[i] = o.d_[i];
+      resize(o.size());
+      copy_elems(data_, o.data_, o.size());
+    }
+    return *this;
+  }
+  SplitVector& operator=(SplitVector&& o) noexcept {
+    if (this != &o) {
+      std::swap(data_, o.data_);
+      std::swap(meta_, o.meta_);
     }
     return *this;
   }
   ~SplitVector() {
-    if (d_) cudaFree(d_);
+    if (data_) cudaFree(data_);
+    if (meta_) cudaFree(meta_);
+    if (d_vec_) cudaFree(d_vec_);
   }
-  T* data() { return d_; }
-  const T* data() const { return d_; }
-  size_t size() const { return size_; }
-  size_t capacity() const { return cap_; }
-  bool empty() const { return size_ == 0; }
-  void reserve(size_t n) {
-    if (n > cap_) reallocate(n);
+
+  // ---- access (host and device) ----
+  __host__ __device__ T* data() noexcept { return data_; }
+  __host__ __device__ const T* data() const noexcept { return data_; }
+  __host__ __device__ const size_t& size() const noexcept { return meta_[0]; }
+  __host__ __device__ size_t capacity() const noexcept { return meta_[1]; }
+  __host__ __device__ bool empty() const noexcept { return size() == 0; }
+  __host__ __device__ T& operator[](size_t i) noexcept { return data_[i]; }
+  __host__ __device__ const T& operator[](size_t i) const noexcept { return data_[i]; }
+  __host__ __device__ T& at(size_t i) { return data_[i]; }
+  __host__ __device__ const T& at(size_t i) const { return data_[i]; }
+  __host__ __device__ T& back() noexcept { return data_[size() - 1]; }
+  __host__ __device__ const T& back() const noexcept { return data_[size() - 1]; }
+  __host__ __device__ T& front() noexcept { return data_[0]; }
+  __host__ __device__ const T& front() const noexcept { return data_[0]; }
+  __host__ __device__ iterator begin() noexcept { return iterator(data_); }
+  __host__ __device__ iterator end() noexcept { return iterator(data_ + size()); }
+  __host__ __device__ const_iterator begin() const noexcept { return const_iterator(data_); }
+  __host__ __device__ const_iterator end() const noexcept { return const_iterator(data_ + size()); }
+  // size_t* of the size word (managed memory): libhx's compactions write a
+  // count there on the device.
+  size_t* size_word() { return meta_; }
+
+  // ---- host-side changes (splitvec.h:720-930, 1032-1060, 1262-1360) ----
+  void reserve(size_t n, bool eco = false, cudaStream_t = 0) {
+    if (!data_) {
+      allocate(n);
+      return;
+    }
+    if (n <= capacity()) return;
+    reallocate(eco ? n : 2 * n);
   }
-  void resize(size_t n, bool /*eco*/ = false) {
-    reserve(n);
-    size_ = n;
+  void resize(size_t n, bool eco = false, cudaStream_t s = 0) {
+    if (n > size()) reserve(n, eco, s);
+    meta_[0] = n;
   }
-  void clear() { size_ = 0; }
+  void grow(cudaStream_t s = 0) { reserve(capacity() + 1, false, s); }
+  void shrink_to_fit(cudaStream_t = 0) {
+    if (data_ && capacity() != size()) reallocate(size());
+  }
+  __host__ __device__ void clear() noexcept { meta_[0] = 0; }
+  __host__ __device__ void remove_from_back(size_t n) noexcept { meta_[0] = size() - n; }
+  __host__ __device__ void pop_back() noexcept {
+    if (size() > 0) remove_from_back(1);
+  }
   void push_back(const T& v) {
-    if (size_ == cap_) reallocate(cap_ ? 2 * cap_ : 8);
-    d_[size_++] = v;
+    if (!data_) {
+      allocate(1);
+      data_[0] = v;
+      return;
+    }
+    resize(size() + 1);
+    data_[size() - 1] = v;
   }
-  T& operator[](size_t i) { return d_[i]; }
-  const T& operator[](size_t i) const { return d_[i]; }
-  T& at(size_t i) { return d_[i]; }
-  T* begin() { return d_; }
-  T* end() { return d_ + size_; }
-  const T* begin() const { return d_; }
-  const T* end() const { return d_ + size_; }
-  void erase(T* first, T* last) {  // erase(range) (splitvec.h:1499): only the tail form is used
-    if (last == end()) size_ = (size_t)(first - d_);
+  template <class... Args>
+  void emplace_back(Args&&... args) {
+    push_back(T(std::forward<Args>(args)...));
   }
-  void optimizeGPU(cudaStream_t = 0) {}
-  void optimizeCPU(cudaStream_t = 0) {}
+  iterator insert(iterator it, const T& v) {
+    const int64_t index = it.data() - data_;
+    if (index < 0 || index > (int64_t)size()) throw std::out_of_range("Insert");
+    const size_t n = size();
+    resize(n + 1);
+    for (int64_t i = (int64_t)n - 1; i >= index; --i) data_[i + 1] = data_[i];
+    data_[index] = v;
+    return iterator(data_ + index);
+  }
+  iterator insert(iterator it, size_t count, const T& v) {
+    const int64_t index = it.data() - data_;
+    if (index < 0 || index > (int64_t)size()) throw std::out_of_range("Insert");
+    const size_t n = size();
+    resize(n + count);
+    for (int64_t i = (int64_t)n - 1; i >= index; --i) data_[i + count] = data_[i];
+    for (size_t k = 0; k < count; ++k) data_[index + k] = v;
+    return iterator(data_ + index);
+  }
+  template <typename InputIterator, class = typename std::enable_if<!std::is_integral<InputIterator>::value>::type>
+  iterator insert(iterator it, InputIterator p0, InputIterator p1) {
+    const int64_t index = it.data() - data_;
+    if (index < 0 || index > (int64_t)size()) throw std::out_of_range("Insert");
+    const size_t count = (size_t)std::distance(p0, p1);
+    const size_t n = size();
+    resize(n + count);
+    for (int64_t i = (int64_t)n - 1; i >= index; --i) data_[i + count] = data_[i];
+    size_t k = 0;
+    for (auto p = p0; p != p1; ++p) data_[index + k++] = *p;
+    return iterator(data_ + index);
+  }
+  /* erase(it) / erase(first, last) (splitvec.h:1472-1520), host and device. */
+  __host__ __device__ iterator erase(iterator it) noexcept {
+    const int64_t index = it.data() - data_;
+    for (size_t i = (size_t)index; i + 1 < size(); ++i) data_[i] = data_[i + 1];
+    meta_[0] = size() - 1;
+    return iterator(data_ + index);
+  }
+  __host__ __device__ iterator erase(iterator p0, iterator p1) noexcept {
+    const int64_t start = p0.data() - data_, stop = p1.data() - data_;
+    const int64_t range = stop - start;
+    const size_t sz = size();
+    for (size_t i = (size_t)start; i + range < sz; ++i) data_[i] = data_[i + range];
+    meta_[0] = sz - range;
+    return iterator(data_ + start);
+  }
+  void swap(SplitVector& o) noexcept {
+    std::swap(data_, o.data_);
+    std::swap(meta_, o.meta_);
+  }
+  /* copyMetadata(SplitInfo*, s) (splitvec.h:568-571). */
+  void copyMetadata(SplitInfo* dst, cudaStream_t s = 0) {
+    hxcompat::check_cuda(cudaMemcpyAsync(&dst->size, &meta_[0], sizeof(size_t), cudaMemcpyDefault, s),
+                         "cudaMemcpyAsync");
+    hxcompat::check_cuda(cudaMemcpyAsync(&dst->capacity, &meta_[1], sizeof(size_t), cudaMemcpyDefault, s),
+                         "cudaMemcpyAsync");
+  }
+  /* upload(s) (splitvec.h:481-491): a device copy of this object for kernels;
+   * it shares the elements, size and capacity. Call it again after any host
+   * call that may reallocate. device_pointer() (:497) returns the last one. */
+  template <bool optimize = true>
+  SplitVector* upload(cudaStream_t s = 0) {
+    if (!d_vec_) hxcompat::check_cuda(cudaMalloc(&d_vec_, sizeof(SplitVector)), "cudaMalloc");
+    hxcompat::check_cuda(cudaMemcpyAsync(d_vec_, this, sizeof(SplitVector), cudaMemcpyHostToDevice, s),
+                         "cudaMemcpyAsync");
+    return d_vec_;
+  }
+  const SplitVector* device_pointer() const noexcept { return d_vec_; }
+  void optimizeGPU(cudaStream_t = 0) noexcept {}
+  void optimizeCPU(cudaStream_t = 0) noexcept {}
+  void memAdvise(cudaMemoryAdvise, int = -1, cudaStream_t = 0) {}
+  void streamAttach(cudaStream_t, uint32_t = cudaMemAttachSingle) {}
+
+  // ---- device-side changes (splitvec.h:902-915, 1070-1100, 1362-1460) ----
+  /* device_push_back: a slot by an atomic increment of the size; fails (and
+   * takes the increment back) when the slot is at capacity - 1 or beyond. */
+  __device__ bool device_push_back(const T& v) {
+    auto* sz = reinterpret_cast<unsigned long long*>(meta_);
+    const unsigned long long old = atomicAdd(sz, 1ull);
+    const size_t cap = meta_[1];
+    if (cap == 0 || old >= cap - 1) {
+      atomicAdd(sz, ~0ull);  // -1
+      return false;
+    }
+    data_[old] = v;
+    return true;
+  }
+  __device__ bool device_push_back(T&& v) {
+    auto* sz = reinterpret_cast<unsigned long long*>(meta_);
+    const unsigned long long old = atomicAdd(sz, 1ull);
+    const size_t cap = meta_[1];
+    if (cap == 0 || old >= cap - 1) {
+      atomicAdd(sz, ~0ull);
+      return false;
+    }
+    data_[old] = std::move(v);
+    return true;
+  }
+  /* device_resize(n, construct): n beyond the capacity is ignored. */
+  __device__ void device_resize(size_t n, bool construct = true) {
+    if (n > capacity()) return;
+    if (construct)
+      for (size_t i = size(); i < n; ++i) data_[i] = T();
+    meta_[0] = n;
+  }
+  template <typename InputIterator, class = typename std::enable_if<!std::is_integral<InputIterator>::value>::type>
+  __device__ iterator device_insert(iterator it, InputIterator p0, InputIterator p1) noexcept {
+    const int64_t count = p1.data() - p0.data();
+    const int64_t index = it.data() - data_;
+    if (count < 0 || index < 0 || index > (int64_t)size() || size() + (size_t)count > capacity()) return end();
+    device_resize(size() + count, false);
+    for (int64_t i = 0; i < count; ++i) data_[index + i] = *(p0.data() + i);
+    return iterator(data_ + index + count);
+  }
+  __device__ iterator device_insert(iterator it, const T& v) noexcept {
+    if (it == end()) {
+      device_push_back(v);
+      return iterator(data_ + size() - 1);
+    }
+    const int64_t index = it.data() - data_;
+    const size_t n = size();
+    if (index < 0 || index > (int64_t)n || n == capacity()) return end();
+    device_resize(n + 1, false);
+    for (int64_t i = (int64_t)n - 1; i >= index; --i) data_[i + 1] = data_[i];
+    data_[index] = v;
+    return iterator(data_ + index);
+  }
+  __device__ iterator device_insert(iterator it, const size_t count, const T& v) {
+    const int64_t index = it.data() - data_;
+    const size_t n = size();
+    if (index < 0 || index > (int64_t)n || n + count > capacity()) return end();
+    device_resize(n + count, false);
+    // elements from index + count on move up by count (in the reference's
+    // order, so a source is read before it is overwritten) ...
+    for (int64_t c = (int64_t)n - 1; c > index && c >= index + (int64_t)count; --c) data_[c + count] = data_[c];
+    // ... and the copies go to [index + count, index + 2 count), inside the new size
+    for (size_t k = 0; k < count && index + count + k < n + count; ++k) data_[index + count + k] = v;
+    return iterator(data_ + index);
+  }
 };
+
+template <typename T, class A>
+inline bool operator==(const SplitVector<T, A>& a, const SplitVector<T, A>& b) {
+  if (a.size() != b.size()) return false;
+  for (size_t i = 0; i < a.size(); ++i)
+    if (!(a[i] == b[i])) return false;
+  return true;
+}
+template <typename T, class A>
+inline bool operator!=(const SplitVector<T, A>& a, const SplitVector<T, A>& b) {
+  return !(a == b);
+}
 
 namespace tools {
 namespace detail {
-
-template <typename T, typename Rule>
-__global__ void count_tiles(const T* in, size_t n, Rule rule, uint32_t* counts) {
-  __shared__ uint32_t s;
-  if (threadIdx.x == 0) s = 0;
-  __syncthreads();
-  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  bool sel = false;
-  if (i < n) {
-    T x = in[i];
-    sel = rule(x);
-  }
-  const unsigned b = __ballot_sync(0xffffffffu, sel);
-  if ((threadIdx.x & 31) == 0 && b) atomicAdd(&s, (uint32_t)__popc(b));
-  __syncthreads();
-  if (threadIdx.x == 0) counts[blockIdx.x] = s;
-}
 
 struct Identity {
   template <typename T>
@@ -193,9 +526,65 @@ struct KeyOf {
   }
 };
 
+// A caller's rule as the selector of the single-pass compaction
+// (hx_stream.cuh). The reference's rules may take their argument by
+// non-const reference, so each call gets a copy of the element (and of the
+// rule, whose call operator need not be const).
+template <typename Rule>
+struct RuleSel {
+  Rule rule;
+  static constexpr bool kRewrites = false;
+  template <class T>
+  __device__ __forceinline__ bool operator()(const T& x) const {
+    Rule r = rule;
+    T y = x;
+    return r(y);
+  }
+  template <class T>
+  __device__ __forceinline__ void rewrite(T*, uint64_t, const T&, bool) const {}
+};
+
+// The first elements of an input that does not start on a 16-byte boundary
+// (fewer than 16 / sizeof(T)), compacted by one thread before the main pass:
+// out[0..h) and the count h in *head, where the main pass starts counting.
 template <typename T, typename O, typename Rule, typename Proj>
-__global__ void scatter_tiles(const T* in, size_t n, Rule rule, const uint32_t* offsets, O* out, size_t cap,
-                              unsigned long long* total, size_t nblocks, Proj proj) {
+__global__ void k_head(const T* in, size_t n, Rule rule, Proj proj, O* out, size_t cap,
+                       unsigned long long* head) {
+  unsigned long long c = 0;
+  for (size_t i = 0; i < n; ++i) {
+    T y = in[i];
+    Rule r = rule;
+    if (r(y)) {
+      if (c < cap) out[c] = proj(in[i]);
+      ++c;
+    }
+  }
+  *head = c;
+}
+
+// Generic path for element sizes that do not divide 16 bytes: per-block
+// counts, libhx's exclusive scan of the counts, then an order-preserving
+// scatter (each block ranks its elements with warp ballots and a warp scan).
+template <typename T, typename Rule>
+__global__ void k_count_blocks(const T* in, size_t n, Rule rule, uint32_t* counts) {
+  __shared__ uint32_t s;
+  if (threadIdx.x == 0) s = 0;
+  __syncthreads();
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  bool sel = false;
+  if (i < n) {
+    T x = in[i];
+    Rule r = rule;
+    sel = r(x);
+  }
+  const unsigned b = __ballot_sync(0xffffffffu, sel);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(&s, (uint32_t)__popc(b));
+  __syncthreads();
+  if (threadIdx.x == 0) counts[blockIdx.x] = s;
+}
+template <typename T, typename O, typename Rule, typename Proj>
+__global__ void k_scatter_blocks(const T* in, size_t n, Rule rule, const uint32_t* offsets, O* out, size_t cap,
+                                 unsigned long long* total, unsigned long long total_max, size_t nblocks, Proj proj) {
   __shared__ uint32_t warp_base[32];
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -203,19 +592,22 @@ __global__ void scatter_tiles(const T* in, size_t n, Rule rule, const uint32_t* 
   T x;
   if (i < n) {
     x = in[i];
-    sel = rule(x);
+    T y = x;
+    Rule r = rule;
+    sel = r(y);
   }
   const unsigned b = __ballot_sync(0xffffffffu, sel);
   if (lane == 0) warp_base[warp] = __popc(b);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t acc = 0;
-    for (unsigned w = 0; w < blockDim.x / 32; ++w) {
-      const uint32_t c = warp_base[w];
-      warp_base[w] = acc;
-      acc += c;
+  if (warp == 0) {
+    const unsigned nw = blockDim.x / 32;
+    const unsigned c = lane < (int)nw ? warp_base[lane] : 0u;
+    const unsigned incl = hxs::warp_incl_scan(c, lane);
+    if (lane < (int)nw) warp_base[lane] = incl - c;
+    if (lane == 31 && blockIdx.x == nblocks - 1) {
+      const unsigned long long t = (unsigned long long)offsets[blockIdx.x] + incl;
+      *total = t < total_max ? t : total_max;
     }
-    if (blockIdx.x == nblocks - 1) *total = (unsigned long long)offsets[blockIdx.x] + acc;
   }
   __syncthreads();
   if (sel) {
@@ -224,27 +616,107 @@ __global__ void scatter_tiles(const T* in, size_t n, Rule rule, const uint32_t* 
   }
 }
 
-// Stable compaction with a user functor: per-block counts, libhx exclusive
-// scan of the counts, order-preserving scatter of proj(x) (the element, or
-// the key of a bucket pair).
+// Device scratch of one compaction of n elements of T. Layout: the kernels'
+// scratch, then 256 bytes of count words at the end (a head count at
+// need - 256, the result count at need - 248). The kernels' part is the
+// single-pass kernel's count slots, or, for element sizes that do not divide
+// 16, the block counts and offsets and libhx's scan scratch.
+template <typename T>
+inline size_t blocks_bytes(size_t n) {
+  const size_t nb = (n + 255) / 256;
+  return ((2 * nb * sizeof(uint32_t) + 255) / 256) * 256;
+}
+template <typename T>
+inline size_t compaction_scratch_bytes(size_t n) {
+  if constexpr (16 % sizeof(T) == 0) {
+    return (((size_t)hxs::scratch_need(n, sizeof(T)) + 255) / 256) * 256 + 256;
+  } else {
+    const size_t nb = (n + 255) / 256;
+    uint64_t sb = 0;
+    hx_scratch_bytes(HX_SCRATCH_SCAN, nb ? nb : 1, &sb);
+    return blocks_bytes<T>(n) + (((size_t)sb + 255) / 256) * 256 + 256;
+  }
+}
+template <typename T>
+inline size_t* result_word(void* scratch, size_t n) {
+  return reinterpret_cast<size_t*>(static_cast<char*>(scratch) + compaction_scratch_bytes<T>(n) - 248);
+}
+
+// Stable compaction with a caller's rule, on the stream, with no host
+// synchronisation: out[0..c) = proj(x) for the selected x in input order
+// (writes at or beyond cap are dropped), and min(c, count_max) to *count.
+// Scratch: `scratch` (at least compaction_scratch_bytes<T>(n) bytes) or, if
+// it is null, a stream-ordered allocation freed on the stream afterwards.
 template <typename T, typename O, typename Rule, typename Proj>
-size_t copy_if_functor(const T* in, O* out, size_t n, size_t cap, Rule rule, Proj proj, cudaStream_t s) {
-  if (n == 0) return 0;
-  const unsigned block = 256;
-  const size_t nb = (n + block - 1) / block;
-  uint32_t* counts = nullptr;
-  unsigned long long* total = nullptr;
-  hxcompat::check_cuda(cudaMallocAsync(&counts, 2 * nb * sizeof(uint32_t) + 16, s), "cudaMallocAsync");
-  uint32_t* offsets = counts + nb;
-  total = reinterpret_cast<unsigned long long*>(counts + 2 * nb);  // 8-byte aligned: 2*nb words
-  count_tiles<<<(unsigned)nb, block, 0, s>>>(in, n, rule, counts);
-  hxcompat::check(hx_exclusive_scan_u32(counts, offsets, nb, nullptr, 0, s), "hx_exclusive_scan_u32");
-  scatter_tiles<<<(unsigned)nb, block, 0, s>>>(in, n, rule, offsets, out, cap, total, nb, proj);
-  unsigned long long h = 0;
-  hxcompat::check_cuda(cudaMemcpyAsync(&h, total, sizeof(h), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
-  hxcompat::check_cuda(cudaFreeAsync(counts, s), "cudaFreeAsync");
+void compact(const T* in, O* out, size_t n, size_t cap, Rule rule, Proj proj, size_t* count, size_t count_max,
+             void* scratch, cudaStream_t s) {
+  static_assert(sizeof(size_t) == sizeof(unsigned long long), "counts are 64-bit");
+  auto* cnt = reinterpret_cast<unsigned long long*>(count);
+  if (n == 0) {
+    hxcompat::check_cuda(cudaMemsetAsync(cnt, 0, sizeof(*cnt), s), "cudaMemsetAsync");
+    return;
+  }
+  const size_t need = compaction_scratch_bytes<T>(n);
+  void* owned = nullptr;
+  if (!scratch) {
+    hxcompat::check_cuda(cudaMallocAsync(&owned, need, s), "cudaMallocAsync");
+    scratch = owned;
+  }
+  if constexpr (16 % sizeof(T) == 0) {
+    auto* head = reinterpret_cast<unsigned long long*>(static_cast<char*>(scratch) + need - 256);
+    const size_t mis = (size_t)(reinterpret_cast<uintptr_t>(in) % 16);
+    if (mis % sizeof(T)) {
+      std::fprintf(stderr, "hashinator_compat: copy_if input is not aligned to its element size\n");
+      std::abort();
+    }
+    const size_t h = std::min(n, mis ? (16 - mis) / sizeof(T) : (size_t)0);
+    if (h) {
+      k_head<<<1, 1, 0, s>>>(in, h, rule, proj, out, cap, head);
+      hxcompat::check_cuda(cudaGetLastError(), "k_head");
+    }
+    if (n > h) {
+      hxs::Done done{cnt, nullptr, nullptr};
+      done.count_max = count_max;
+      done.base_from = h ? head : nullptr;
+      hxcompat::check_cuda(hxs::launch<T, O, RuleSel<Rule>, false>(in + h, out, n - h, RuleSel<Rule>{rule}, cap,
+                                                                  done, scratch, s),
+                           "single-pass compaction");
+    } else {  // fewer elements than one 16-byte group: the head is everything
+      hxcompat::check_cuda(cudaMemcpyAsync(cnt, head, sizeof(*cnt), cudaMemcpyDeviceToDevice, s), "cudaMemcpyAsync");
+    }
+  } else {
+    const unsigned block = 256;
+    const size_t nb = (n + block - 1) / block;
+    auto* counts = static_cast<uint32_t*>(scratch);
+    uint32_t* offsets = counts + nb;
+    void* scan_scratch = static_cast<char*>(scratch) + blocks_bytes<T>(n);
+    uint64_t sb = 0;
+    hx_scratch_bytes(HX_SCRATCH_SCAN, nb, &sb);
+    k_count_blocks<<<(unsigned)nb, block, 0, s>>>(in, n, rule, counts);
+    hxcompat::check(hx_exclusive_scan_u32(counts, offsets, nb, scan_scratch, sb, s), "hx_exclusive_scan_u32");
+    k_scatter_blocks<<<(unsigned)nb, block, 0, s>>>(in, n, rule, offsets, out, cap, cnt, count_max, nb, proj);
+    hxcompat::check_cuda(cudaGetLastError(), "k_scatter_blocks");
+  }
+  if (owned) hxcompat::check_cuda(cudaFreeAsync(owned, s), "cudaFreeAsync");
+}
+
+// The same with the count read back on the host (synchronises the stream,
+// as the reference's copy_if does). With caller scratch no allocation is made.
+template <typename T, typename O, typename Rule, typename Proj>
+size_t compact_sync(const T* in, O* out, size_t n, size_t cap, Rule rule, Proj proj, void* scratch, cudaStream_t s) {
+  const size_t need = compaction_scratch_bytes<T>(n);
+  void* owned = nullptr;
+  if (!scratch) {
+    hxcompat::check_cuda(cudaMallocAsync(&owned, need, s), "cudaMallocAsync");
+    scratch = owned;
+  }
+  size_t* d = result_word<T>(scratch, n);
+  compact(in, out, n, cap, rule, proj, d, ~(size_t)0, scratch, s);
+  size_t h = 0;
+  hxcompat::check_cuda(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+  if (owned) hxcompat::check_cuda(cudaFreeAsync(owned, s), "cudaFreeAsync");
   hxcompat::check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
-  return (size_t)h;
+  return h;
 }
 
 template <typename T>
@@ -254,37 +726,12 @@ constexpr int elem_bytes() {
 
 }  // namespace detail
 
-/* copy_if(in, out, rule, stream) (split_tools.h:1129): out gets the selected
- * elements in order and is resized to their count. */
-template <typename T, typename Rule>
-void copy_if(SplitVector<T>& input, SplitVector<T>& output, Rule rule, cudaStream_t s = 0) {
-  size_t c;
-  if constexpr (std::is_same<Rule, hx_pred>::value) {
-    uint64_t h = 0;
-    const hx_status st = hx_copy_if(input.data(), output.data(), input.size(), detail::elem_bytes<T>(), &rule,
-                                    output.size(), nullptr, &h, nullptr, 0, s);
-    if (st != HX_OK && st != HX_ERR_CAPACITY) hxcompat::check(st, "hx_copy_if");
-    c = (size_t)h;
-  } else {
-    c = detail::copy_if_functor(input.data(), output.data(), input.size(), output.size(), rule, detail::Identity{},
-                                s);
-  }
-  output.erase(output.data() + (c < output.size() ? c : output.size()), output.end());
-}
-
-/* copy_if(T* in, T* out, size, rule, stack, max_size, stream)
- * (split_tools.h:1211): returns the count. */
-template <typename T, typename Rule>
-size_t copy_if(T* input, T* output, size_t size, Rule rule, void* /*stack*/, size_t /*max_size*/, cudaStream_t s = 0) {
-  return detail::copy_if_functor(input, output, size, size, rule, detail::Identity{}, s);
-}
-
 /* splitStackArena (split_tools.h:491-535): a bump allocator over one device
  * buffer, either allocated stream-ordered (and freed with the arena) or
- * borrowed from the caller. libhx's compaction takes its scratch from the
- * device's stream-ordered pool itself, so the copy_if / copy_keys_if
- * overloads below accept an arena or a (stack, max_size) buffer for source
- * compatibility and leave it untouched. */
+ * borrowed from the caller. The copy_if / copy_keys_if overloads that take
+ * an arena or a (stack, max_size) buffer take their device scratch from it
+ * and allocate nothing; like the reference's, the arena aborts with a message
+ * when it has too little room (size it with estimateMemoryForCompaction). */
 class splitStackArena {
   void* base_ = nullptr;
   size_t cap_ = 0, used_ = 0;
@@ -319,70 +766,191 @@ class splitStackArena {
 };
 
 /* estimateMemoryForCompaction (split_tools.h:1065-1090): the device scratch
- * that libhx's compaction of inputSize elements uses (hx_scratch_bytes). */
+ * that one compaction of inputSize elements takes from an arena here — enough
+ * for libhx's descriptor rules and for a functor rule over elements of 4, 8
+ * or 16 bytes (the typed form also covers its own element size). */
 template <int BLOCKSIZE = 1024>
 [[nodiscard]] size_t estimateMemoryForCompaction(const size_t inputSize) noexcept {
   uint64_t b = 0;
-  return hx_scratch_bytes(HX_SCRATCH_COPY_IF, inputSize, &b) == HX_OK ? (size_t)b : 0;
+  const size_t lib = hx_scratch_bytes(HX_SCRATCH_COPY_IF, inputSize, &b) == HX_OK ? (size_t)b : 0;
+  const size_t fun = detail::compaction_scratch_bytes<uint32_t>(inputSize);
+  return ((std::max(lib, fun) + 255) / 256) * 256 + 256;  // + room to align the piece taken from an arena
 }
 template <typename T, int BLOCKSIZE = 1024>
 [[nodiscard]] size_t estimateMemoryForCompaction(const SplitVector<T>& input) noexcept {
-  return estimateMemoryForCompaction<BLOCKSIZE>(input.size());
+  const size_t n = input.size();
+  return std::max(estimateMemoryForCompaction<BLOCKSIZE>(n),
+                  ((detail::compaction_scratch_bytes<T>(n) + 255) / 256) * 256 + 256);
 }
 
-/* copy_if(in, out, rule, splitStackArena&&, stream) (split_tools.h:1162)
- * and copy_if(in, out, rule, stack, max_size, stream) (:1194). */
-template <typename T, typename Rule>
-void copy_if(SplitVector<T>& input, SplitVector<T>& output, Rule rule, splitStackArena&& /*mPool*/,
-             cudaStream_t s = 0) {
-  copy_if(input, output, rule, s);
+namespace detail {
+// One compaction of `input` into `output` (a SplitVector), the count written
+// into output's size word on the device (at most count_max), from `scratch`
+// (or stream-ordered scratch when it is null). Rules are functors (the
+// kernel here) or hx_pred descriptors (libhx, then the count is copied into
+// the size word).
+template <int = 0>  // a template, so that every translation unit may define it
+__global__ void k_set_size(const unsigned long long* c, size_t* size_word, size_t count_max) {
+  const unsigned long long v = *c;
+  *size_word = v < count_max ? (size_t)v : count_max;
 }
+template <typename T, typename O, typename Rule, typename Proj>
+void compact_into(const T* in, size_t n, O* out, size_t cap, Rule rule, Proj proj, size_t* size_word,
+                  size_t count_max, void* scratch, size_t scratch_bytes, cudaStream_t s) {
+  if constexpr (std::is_same<Rule, hx_pred>::value) {
+    static_assert(std::is_same<T, O>::value, "descriptor rules copy whole elements: use a functor for keys");
+    uint64_t need = 0;
+    hxcompat::check(hx_scratch_bytes(HX_SCRATCH_COPY_IF, n, &need), "hx_scratch_bytes");
+    void* owned = nullptr;
+    if (!scratch) {
+      hxcompat::check_cuda(cudaMallocAsync(&owned, need + 256, s), "cudaMallocAsync");
+      scratch = owned;
+    } else if (scratch_bytes < need + 256) {
+      std::fprintf(stderr, "hashinator_compat: %zu scratch bytes given, %zu needed\n", scratch_bytes,
+                   (size_t)need + 256);
+      std::abort();
+    }
+    auto* c = reinterpret_cast<uint64_t*>(static_cast<char*>(scratch) + need);
+    const hx_status st = hx_copy_if(in, out, n, elem_bytes<T>(), &rule, cap, c, nullptr, scratch, need, s);
+    hxcompat::check(st, "hx_copy_if");
+    k_set_size<><<<1, 1, 0, s>>>(reinterpret_cast<const unsigned long long*>(c), size_word, count_max);
+    hxcompat::check_cuda(cudaGetLastError(), "k_set_size");
+    if (owned) hxcompat::check_cuda(cudaFreeAsync(owned, s), "cudaFreeAsync");
+  } else {
+    if (scratch && scratch_bytes < compaction_scratch_bytes<T>(n)) {
+      std::fprintf(stderr, "hashinator_compat: %zu scratch bytes given, %zu needed\n", scratch_bytes,
+                   compaction_scratch_bytes<T>(n));
+      std::abort();
+    }
+    compact(in, out, n, cap, rule, proj, size_word, count_max, scratch, s);
+  }
+}
+// A 256-byte-aligned piece of `need` bytes from an arena (it takes need + 256).
+inline void* take_aligned(splitStackArena& pool, size_t need) {
+  const uintptr_t p = reinterpret_cast<uintptr_t>(pool.allocate(need + 256));
+  return reinterpret_cast<void*>((p + 255) / 256 * 256);
+}
+// Bytes one compaction of n elements of T with this rule takes from an arena.
 template <typename T, typename Rule>
-void copy_if(SplitVector<T>& input, SplitVector<T>& output, Rule rule, void* /*stack*/, size_t /*max_size*/,
+inline size_t scratch_for(size_t n) {
+  if constexpr (std::is_same<Rule, hx_pred>::value) {
+    uint64_t need = 0;
+    hx_scratch_bytes(HX_SCRATCH_COPY_IF, n, &need);
+    return (size_t)need + 256;
+  } else {
+    return compaction_scratch_bytes<T>(n);
+  }
+}
+// The loop forms' compaction: the input's size is read on the device (its
+// capacity bounds it), output written into its capacity, its size set on the
+// device; no host synchronisation. Descriptor rules and element sizes that
+// do not divide 16 take the input's size as the host sees it.
+template <typename T, class A, typename U, class B, typename Rule, typename Proj>
+void compact_loop(SplitVector<T, A>& in, SplitVector<U, B>& out, Rule rule, Proj proj, cudaStream_t s) {
+  constexpr bool single_pass = !std::is_same<Rule, hx_pred>::value && (16 % sizeof(T) == 0);
+  if constexpr (single_pass) {
+    const size_t nmax = in.capacity();
+    if (nmax == 0 || !in.data()) {
+      hxcompat::check_cuda(cudaMemsetAsync(out.size_word(), 0, sizeof(size_t), s), "cudaMemsetAsync");
+      return;
+    }
+    void* sc = nullptr;
+    hxcompat::check_cuda(cudaMallocAsync(&sc, compaction_scratch_bytes<T>(nmax), s), "cudaMallocAsync");
+    hxs::Done done{reinterpret_cast<unsigned long long*>(out.size_word()), nullptr, nullptr};
+    done.count_max = out.capacity();
+    done.n_from = reinterpret_cast<const unsigned long long*>(in.size_word());
+    hxcompat::check_cuda(hxs::launch<T, U, RuleSel<Rule>, false>(in.data(), out.data(), nmax, RuleSel<Rule>{rule},
+                                                                out.capacity(), done, sc, s),
+                         "single-pass compaction");
+    hxcompat::check_cuda(cudaFreeAsync(sc, s), "cudaFreeAsync");
+  } else {
+    compact_into(in.data(), in.size(), out.data(), out.capacity(), rule, proj, out.size_word(), out.capacity(),
+                 nullptr, 0, s);
+  }
+}
+}  // namespace detail
+
+/* copy_if(in, out, rule, stream) (split_tools.h:1129): out gets the selected
+ * elements in order and is resized to their count (out must hold them, as in
+ * the reference); blocks until done, as the reference does. One pass over
+ * the input (hx_stream.cuh) for a functor rule, libhx for an hx_pred. */
+template <typename T, class A, typename Rule>
+void copy_if(SplitVector<T, A>& input, SplitVector<T, A>& output, Rule rule, cudaStream_t s = 0) {
+  detail::compact_into(input.data(), input.size(), output.data(), output.size(), rule, detail::Identity{},
+                       output.size_word(), output.size(), nullptr, 0, s);
+  hxcompat::check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+}
+/* copy_if(in, out, rule, splitStackArena&&, stream) (split_tools.h:1162)
+ * and copy_if(in, out, rule, stack, max_size, stream) (:1194): the scratch
+ * comes from the arena or the caller's buffer; nothing is allocated. */
+template <typename T, class A, typename Rule>
+void copy_if(SplitVector<T, A>& input, SplitVector<T, A>& output, Rule rule, splitStackArena&& pool,
              cudaStream_t s = 0) {
-  copy_if(input, output, rule, s);
+  const size_t need = detail::scratch_for<T, Rule>(input.size());
+  void* sc = detail::take_aligned(pool, need);
+  detail::compact_into(input.data(), input.size(), output.data(), output.size(), rule, detail::Identity{},
+                       output.size_word(), output.size(), sc, need, s);
+  hxcompat::check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  pool.deallocate(need + 256);
+}
+template <typename T, class A, typename Rule>
+void copy_if(SplitVector<T, A>& input, SplitVector<T, A>& output, Rule rule, void* stack, size_t max_size,
+             cudaStream_t s = 0) {
+  copy_if(input, output, rule, splitStackArena(stack, max_size), s);
+}
+/* copy_if(T* in, T* out, size, rule, stack, max_size, stream)
+ * (split_tools.h:1211): returns the count; scratch from the caller's buffer. */
+template <typename T, typename Rule>
+size_t copy_if(T* input, T* output, size_t size, Rule rule, void* stack, size_t max_size, cudaStream_t s = 0) {
+  splitStackArena pool(stack, max_size);
+  void* sc = detail::take_aligned(pool, detail::compaction_scratch_bytes<T>(size));
+  return detail::compact_sync(input, output, size, size, rule, detail::Identity{}, sc, s);
 }
 
 /* copy_keys_if(in, out, rule, stream) (split_tools.h:1095) and its arena
  * (:1147) and stack (:1177) forms: the keys of the selected hash_pairs, in
- * order; out must hold the result and is resized to the count. The rule is
- * a functor over the pair. */
-template <typename T, typename U, typename Rule>
-void copy_keys_if(SplitVector<T>& input, SplitVector<U>& output, Rule rule, cudaStream_t s = 0) {
-  const size_t c = detail::copy_if_functor(input.data(), output.data(), input.size(), output.size(), rule,
-                                           detail::KeyOf{}, s);
-  output.erase(output.data() + (c < output.size() ? c : output.size()), output.end());
+ * order; out must hold the result and is resized to the count. */
+template <typename T, class A, typename U, class B, typename Rule>
+void copy_keys_if(SplitVector<T, A>& input, SplitVector<U, B>& output, Rule rule, cudaStream_t s = 0) {
+  detail::compact_into(input.data(), input.size(), output.data(), output.size(), rule, detail::KeyOf{},
+                       output.size_word(), output.size(), nullptr, 0, s);
+  hxcompat::check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
 }
-template <typename T, typename U, typename Rule>
-void copy_keys_if(SplitVector<T>& input, SplitVector<U>& output, Rule rule, splitStackArena&& /*mPool*/,
+template <typename T, class A, typename U, class B, typename Rule>
+void copy_keys_if(SplitVector<T, A>& input, SplitVector<U, B>& output, Rule rule, splitStackArena&& pool,
                   cudaStream_t s = 0) {
-  copy_keys_if(input, output, rule, s);
+  const size_t need = detail::compaction_scratch_bytes<T>(input.size());
+  void* sc = detail::take_aligned(pool, need);
+  detail::compact_into(input.data(), input.size(), output.data(), output.size(), rule, detail::KeyOf{},
+                       output.size_word(), output.size(), sc, need, s);
+  hxcompat::check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  pool.deallocate(need + 256);
 }
-template <typename T, typename U, typename Rule>
-void copy_keys_if(SplitVector<T>& input, SplitVector<U>& output, Rule rule, void* /*stack*/, size_t /*max_size*/,
+template <typename T, class A, typename U, class B, typename Rule>
+void copy_keys_if(SplitVector<T, A>& input, SplitVector<U, B>& output, Rule rule, void* stack, size_t max_size,
                   cudaStream_t s = 0) {
-  copy_keys_if(input, output, rule, s);
+  copy_keys_if(input, output, rule, splitStackArena(stack, max_size), s);
 }
 
-/* copy_if_loop / copy_if_keys_loop (split_tools.h:995-1020): the reference's
- * single-block compactions, which write into the output's capacity and set
- * its size on the device. Here they run copy_if / copy_keys_if into the
- * output's capacity and set its size on the host; the elements and the size
- * are the same once the stream has finished. */
-template <typename T, typename Rule>
-void copy_if_loop(SplitVector<T>& input, SplitVector<T>& output, Rule rule, cudaStream_t s = 0) {
-  output.resize(output.capacity());
-  copy_if(input, output, rule, s);
+/* copy_if_loop / copy_if_keys_loop (split_tools.h:997-1020, the single-block
+ * loop_compact of :719-799): no host synchronisation — the input's size is
+ * read on the device, the selected elements (or keys) are written into the
+ * output's capacity, and the output's size is set on the device to their
+ * count (at most the capacity). Scratch is stream-ordered. */
+template <typename T, class A, typename Rule>
+void copy_if_loop(SplitVector<T, A>& input, SplitVector<T, A>& output, Rule rule, cudaStream_t s = 0) {
+  detail::compact_loop(input, output, rule, detail::Identity{}, s);
 }
-template <typename T, typename U, typename Rule>
-void copy_if_keys_loop(SplitVector<T>& input, SplitVector<U>& output, Rule rule, cudaStream_t s = 0) {
-  output.resize(output.capacity());
-  copy_keys_if(input, output, rule, s);
+template <typename T, class A, typename U, class B, typename Rule>
+void copy_if_keys_loop(SplitVector<T, A>& input, SplitVector<U, B>& output, Rule rule, cudaStream_t s = 0) {
+  detail::compact_loop(input, output, rule, detail::KeyOf{}, s);
 }
 
 /* split_prefix_scan(in, out, stream) (split_tools.h:363): exclusive sum of
  * uint32_t, any length (the reference asserts a power of two). */
-inline void split_prefix_scan(SplitVector<uint32_t>& input, SplitVector<uint32_t>& output, cudaStream_t s = 0) {
+template <class A>
+inline void split_prefix_scan(SplitVector<uint32_t, A>& input, SplitVector<uint32_t, A>& output,
+                              cudaStream_t s = 0) {
   output.resize(input.size());
   hxcompat::check(hx_exclusive_scan_u32(input.data(), output.data(), input.size(), nullptr, 0, s),
                   "hx_exclusive_scan_u32");
@@ -416,6 +984,46 @@ class Hashmap {
   hx_map* map() const {
     static_assert(kDefaultSentinels, "libhx operates only on tables with the default sentinels");
     return m_;
+  }
+  // The rule of extractLoop / extractAllKeys (hashinator.h:1195-1197, 1239-1241).
+  using ValidKey = hxcompat::ValidKeyRule<hash_pair<KEY_TYPE, VAL_TYPE>, KEY_TYPE, EMPTYBUCKET, TOMBSTONE>;
+  // extractKeysByPattern's body: the keys of the selected buckets into
+  // `elements`, resized to the count; scratch from (stack, max_size) if given.
+  template <typename Rule>
+  size_t extract_keys(split::SplitVector<KEY_TYPE>& elements, Rule rule, void* stack, size_t max_size,
+                      cudaStream_t s) {
+    void* b = nullptr;
+    uint64_t nb = 0;
+    hxcompat::check(hx_bucket_data(map(), &b, &nb), "hx_bucket_data");
+    elements.resize(nb);
+    if constexpr (std::is_same<Rule, hx_pred>::value) {
+      uint64_t h = 0;
+      const hx_status st = hx_extract_keys(map(), &rule, elements.data(), nb, nullptr, &h, s);
+      if (st != HX_OK && st != HX_ERR_CAPACITY) hxcompat::check(st, "hx_extract_keys");
+      elements.erase(elements.data() + h, elements.end());
+      return (size_t)h;
+    } else {
+      void* sc = nullptr;
+      const size_t need = split::tools::detail::compaction_scratch_bytes<pair_t>((size_t)nb);
+      if (stack) {
+        split::tools::splitStackArena pool(stack, max_size);
+        sc = split::tools::detail::take_aligned(pool, need);
+      }
+      split::tools::detail::compact(static_cast<const pair_t*>(b), elements.data(), (size_t)nb, (size_t)nb, rule,
+                                    split::tools::detail::KeyOf{}, elements.size_word(), (size_t)nb, sc, s);
+      sync(s);
+      return elements.size();
+    }
+  }
+  // The loop forms' body: into `elements`' capacity, its size set on the device.
+  template <typename Rule, typename Proj, typename U>
+  void loop_into(split::SplitVector<U>& elements, Rule rule, Proj proj, cudaStream_t s) {
+    void* b = nullptr;
+    uint64_t nb = 0;
+    hxcompat::check(hx_bucket_data(map(), &b, &nb), "hx_bucket_data");
+    split::tools::detail::compact_into(static_cast<const pair_t*>(b), (size_t)nb, elements.data(),
+                                       elements.capacity(), rule, proj, elements.size_word(), elements.capacity(),
+                                       nullptr, 0, s);
   }
   __host__ __device__ view_t view() const {
     static_assert(kDefaultSentinels, "libhx operates only on tables with the default sentinels");
@@ -508,45 +1116,32 @@ class Hashmap {
   }
 
   /* extractKeysByPattern(SplitVector<KEY>&, Rule, s) (hashinator.h:1199):
-   * the keys of the buckets where the rule holds, in bucket order. */
+   * the keys of the buckets where the rule holds, in bucket order; blocks.
+   * A functor rule runs the single-pass compaction in this translation unit
+   * (one read of the buckets); an hx_pred runs inside libhx. */
   template <bool prefetches = true, typename Rule>
   size_t extractKeysByPattern(split::SplitVector<KEY_TYPE>& elements, Rule rule, cudaStream_t s = 0) {
-    void* b = nullptr;
-    uint64_t nb = 0;
-    hxcompat::check(hx_bucket_data(map(), &b, &nb), "hx_bucket_data");
-    elements.resize(nb);
-    size_t c;
-    if constexpr (std::is_same<Rule, hx_pred>::value) {
-      uint64_t h = 0;
-      const hx_status st = hx_extract_keys(map(), &rule, elements.data(), nb, nullptr, &h, s);
-      if (st != HX_OK && st != HX_ERR_CAPACITY) hxcompat::check(st, "hx_extract_keys");
-      c = (size_t)h;
-    } else {
-      c = split::tools::detail::copy_if_functor(static_cast<pair_t*>(b), elements.data(), nb, nb, rule,
-                                                split::tools::detail::KeyOf{}, s);
-    }
-    elements.erase(elements.data() + c, elements.end());
-    return c;
+    return extract_keys(elements, rule, nullptr, 0, s);
   }
+  /* extractKeysByPattern(keys, rule, stack, max_size, s) (hashinator.h:1218):
+   * the scratch comes from the caller's buffer; nothing is allocated. */
   template <bool prefetches = true, typename Rule>
-  size_t extractKeysByPattern(split::SplitVector<KEY_TYPE>& elements, Rule rule, void* /*stack*/,
-                              size_t /*max_size*/, cudaStream_t s = 0) {
-    return extractKeysByPattern<prefetches>(elements, rule, s);
+  size_t extractKeysByPattern(split::SplitVector<KEY_TYPE>& elements, Rule rule, void* stack, size_t max_size,
+                              cudaStream_t s = 0) {
+    return extract_keys(elements, rule, stack, max_size, s);
   }
-  /* extractAllKeys(SplitVector<KEY>&, s) (hashinator.h:1224). */
+  /* extractAllKeys(SplitVector<KEY>&, s) (hashinator.h:1236) and its stack form (:1244). */
   template <bool prefetches = true>
   size_t extractAllKeys(split::SplitVector<KEY_TYPE>& elements, cudaStream_t s = 0) {
-    hx_pred p{HX_PRED_VALID, HX_FIELD_KEY, 0, 0, 0, 0};
-    return extractKeysByPattern<prefetches>(elements, p, s);
+    return extract_keys(elements, ValidKey{}, nullptr, 0, s);
   }
   template <bool prefetches = true>
-  size_t extractAllKeys(split::SplitVector<KEY_TYPE>& elements, void* /*stack*/, size_t /*max_size*/,
-                        cudaStream_t s = 0) {
-    return extractAllKeys<prefetches>(elements, s);
+  size_t extractAllKeys(split::SplitVector<KEY_TYPE>& elements, void* stack, size_t max_size, cudaStream_t s = 0) {
+    return extract_keys(elements, ValidKey{}, stack, max_size, s);
   }
 
   /* extractPattern(hash_pair*, Rule, stream) (hashinator.h:1168): bucket
-   * order; the output must hold the result. */
+   * order; the output must hold the result; returns the count (blocks). */
   template <typename Rule>
   size_t extractPattern(pair_t* elements, Rule rule, cudaStream_t s = 0) {
     void* b = nullptr;
@@ -558,8 +1153,8 @@ class Hashmap {
       if (st != HX_OK && st != HX_ERR_CAPACITY) hxcompat::check(st, "hx_extract_pattern");
       return (size_t)c;
     } else {
-      return split::tools::detail::copy_if_functor(static_cast<pair_t*>(b), elements, nb, nb, rule,
-                                                   split::tools::detail::Identity{}, s);
+      return split::tools::detail::compact_sync(static_cast<const pair_t*>(b), elements, (size_t)nb, (size_t)nb,
+                                                rule, split::tools::detail::Identity{}, nullptr, s);
     }
   }
   /* extractPattern(SplitVector&, Rule, stream) (hashinator.h:1155): resized
@@ -655,22 +1250,25 @@ class Hashmap {
     std::printf("\n");
   }
 
-  /* The single-block "loop" extractions (hashinator.h:1187-1260) keep their
-   * count on the device in the reference; here they run the same selection
-   * as extractPattern / extractKeysByPattern and size `elements` on the
-   * host, so the elements are the same once the stream has finished. */
+  /* The single-block "loop" extractions (hashinator.h:1187-1260): no host
+   * synchronisation. The selection is written into `elements`' capacity and
+   * its size is set on the device to the count (at most the capacity), as
+   * the reference's loop_compact does; read elements.size() after the stream
+   * has finished. Scratch is stream-ordered. */
   template <typename Rule>
   void extractPatternLoop(split::SplitVector<pair_t>& elements, Rule rule, cudaStream_t s = 0) {
-    extractPattern(elements, rule, s);
+    loop_into(elements, rule, split::tools::detail::Identity{}, s);
   }
   void extractLoop(split::SplitVector<pair_t>& elements, cudaStream_t s = 0) {
-    extractPattern(elements, hx_pred{HX_PRED_VALID, HX_FIELD_KEY, 0, 0, 0, 0}, s);
+    loop_into(elements, ValidKey{}, split::tools::detail::Identity{}, s);
   }
   template <typename Rule>
   void extractKeysByPatternLoop(split::SplitVector<KEY_TYPE>& elements, Rule rule, cudaStream_t s = 0) {
-    extractKeysByPattern(elements, rule, s);
+    loop_into(elements, rule, split::tools::detail::KeyOf{}, s);
   }
-  void extractAllKeysLoop(split::SplitVector<KEY_TYPE>& elements, cudaStream_t s = 0) { extractAllKeys(elements, s); }
+  void extractAllKeysLoop(split::SplitVector<KEY_TYPE>& elements, cudaStream_t s = 0) {
+    loop_into(elements, ValidKey{}, split::tools::detail::KeyOf{}, s);
+  }
 
   // ---- device API (hashinator.h:853-1126, 1417-1769) ----
   /* upload(s) (hashinator.h:1417): a device copy of this map for kernels;

@@ -322,6 +322,28 @@ hx_status hx_batch_run_graph(hx_batch_plan* plan, hx_stream stream);
 /* The plain path: the per-map launches of hx_insert, hx_retrieve, hx_erase
  * and hx_clean_tombstones for every map in turn. */
 hx_status hx_batch_run_per_map(hx_batch_plan* plan, hx_stream stream);
+/* Autotuner (no reference counterpart): times the plan's captured-graph
+ * replay (hx_batch_run_graph, the launch the product runs) over the grid
+ * group_widths x block_sizes x tile_keys (NULL arrays: {1,4,8,16,32} x
+ * {128,256,512} x {512,2048,8192}); for each point one warm-up replay and
+ * then `reps` timed replays (CUDA events on `stream`), each after `reset`
+ * has restored the maps to the state the round starts from (reset = NULL:
+ * hx_batch_clear, for a round that starts from empty maps). Leaves the plan
+ * on the fastest point and the maps reset; writes up to trials_capacity
+ * trials (milliseconds = the fastest timed replay of each point) and the
+ * best one. Synchronises. A trial whose bounded waits ran out ends the
+ * search with HX_ERR_TIMEOUT. */
+typedef struct hx_batch_trial {
+  int32_t group_width;
+  int32_t block_size;
+  int32_t tile_keys;
+  float ms;
+} hx_batch_trial;
+typedef hx_status (*hx_batch_reset_fn)(void* user, hx_stream stream);
+hx_status hx_batch_autotune(hx_batch_plan* plan, const int32_t* group_widths, uint32_t n_groups,
+                            const int32_t* block_sizes, uint32_t n_blocks, const int32_t* tile_keys, uint32_t n_tiles,
+                            int reps, hx_batch_reset_fn reset, void* reset_user, hx_stream stream,
+                            hx_batch_trial* trials, uint32_t trials_capacity, hx_batch_trial* best);
 /* Error word of the last fused run (synchronises): 0 ok, 1 a bounded wait ran
  * out (HX_ERR_TIMEOUT), 2 a moved list overflowed (HX_ERR_CAPACITY). */
 hx_status hx_batch_check(hx_batch_plan* plan, int32_t* error, hx_stream stream);

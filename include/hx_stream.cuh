@@ -1,0 +1,507 @@
+// hx_stream.cuh — phase-partitioned streaming kernels: stable stream
+// compaction (copy_if, extractPattern, the clean_tombstones pass) and the
+// exclusive u32 scan, for 16-byte-aligned inputs.
+//
+// Header-only so that the drop-in C++ header can instantiate the same
+// compaction for a caller's own `Rule` functor in the caller's translation
+// unit; libhx instantiates it for its predicate descriptors.
+//
+// Shape. One cooperative launch of G co-resident CTAs (G = resident CTAs per
+// SM x SMs). The input is cut into slices of SLICE elements (one stage of
+// shared memory, 16 KiB by default); phase p gives slice p*G + b to CTA b, so
+// a phase is G consecutive slices. Each CTA keeps STAGES slices in flight,
+// each filled by one bulk copy (cp.async.bulk, completion on an mbarrier).
+//   pass 1, phase p: read the slice from shared memory, evaluate the rule (or
+//     sum, for the scan), write the CTA-local result back into the same stage
+//     (the selected elements packed at the front, or the local exclusive
+//     sums), and publish the CTA's count for phase p in a slot of scratch.
+//   pass 2, phase p - D (D phases later): read every CTA's count of that
+//     phase, which by then are almost always published, add up those of the
+//     CTAs before this one and of all earlier phases, write the stage's result
+//     to global memory at that offset, and refill the stage with a later slice.
+// So the input is read once, the output written once, the only exchange
+// between CTAs is one count per CTA per phase, and its latency is hidden
+// behind D phases of work instead of sitting on every tile's critical path
+// as in a decoupled look-back.
+//
+// Co-residency: every CTA waits for the counts of every other, so the launch
+// is cooperative (the runtime guarantees all CTAs resident). Every wait is
+// still bounded: an mbarrier wait or a count wait that runs out (about one
+// second) sets the scratch error word; every CTA that sees the error word
+// stops, waits (bounded) for the bulk copies it issued, and returns.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <atomic>
+#include <type_traits>
+
+namespace hxs {
+
+// ---- PTX helpers --------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+constexpr unsigned long long kWaitNs = 1000000000ull;  // about one second per wait
+// Waits for the phase of `bar` with `parity`; false after about a second.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+  if (mbar_try(bar, parity)) return true;
+  const unsigned long long t0 = globaltimer();
+  for (unsigned i = 0; i < (1u << 26); ++i) {
+    if (mbar_try(bar, parity)) return true;
+    if ((i & 255) == 255 && globaltimer() - t0 > kWaitNs) return false;
+  }
+  return false;
+}
+// One bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned)
+// from global into shared memory, completing `bytes` transactions on `bar`.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned warp_incl_scan(unsigned x, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  return x;
+}
+
+// ---- geometry and scratch -------------------------------------------------
+#ifndef HX_STREAM_R
+#define HX_STREAM_R 4  // uint4 per thread per slice: 256 threads x 4 x 16 B = 16 KiB slices
+#endif
+#ifndef HX_STREAM_STAGES
+#define HX_STREAM_STAGES 6
+#endif
+#ifndef HX_STREAM_DEFER
+#define HX_STREAM_DEFER 2
+#endif
+constexpr int kBlock = 256;
+constexpr int kR = HX_STREAM_R;
+constexpr int kStages = HX_STREAM_STAGES;
+constexpr int kDefer = HX_STREAM_DEFER;
+static_assert(kDefer >= 1 && kDefer < kStages, "a stage must be free to load while D phases wait");
+// Count slots per CTA: a CTA overwrites the slot of phase p - kSlots only
+// after every CTA has read it (see the kernel), which needs 2 * D + 2 slots.
+constexpr int kSlots = 2 * kDefer + 2;
+constexpr int kMaxGrid = 2048;
+constexpr unsigned kSliceBytes = kBlock * kR * 16;
+
+// Scratch: [error word u32][pad .. 256 B][count slots u64 x kSlots x grid].
+// The launcher zeroes the part it uses.
+constexpr uint64_t kScratchBytes = 256 + 8ull * kSlots * kMaxGrid;
+inline uint64_t scratch_bytes_used(unsigned grid) { return 256 + 8ull * kSlots * grid; }
+// Scratch a pass over n elements of elem_bytes each needs: its grid is at
+// most one CTA per slice.
+inline uint64_t scratch_need(uint64_t n, unsigned elem_bytes) {
+  uint64_t slices = (n * elem_bytes + kSliceBytes - 1) / kSliceBytes;
+  if (slices < 1) slices = 1;
+  if (slices > (uint64_t)kMaxGrid) slices = kMaxGrid;
+  return scratch_bytes_used((unsigned)slices);
+}
+
+struct Scratch {
+  unsigned* error;
+  unsigned long long* slots;
+};
+inline Scratch carve(void* p) {
+  Scratch s;
+  s.error = reinterpret_cast<unsigned*>(p);
+  s.slots = reinterpret_cast<unsigned long long*>(static_cast<char*>(p) + 256);
+  return s;
+}
+
+// What a selected element writes: the element, or only the key of a pair.
+template <class T, class O>
+__device__ __forceinline__ O project(const T& x) {
+  if constexpr (std::is_same<T, O>::value) return x;
+  else return x.first;
+}
+
+// Selector concept (compaction): a copyable struct with
+//   __device__ bool operator()(const T& x) const;
+//   static constexpr bool kRewrites;   // true: called as below for every element of the input
+//   __device__ void rewrite(T* in, uint64_t i, const T& x, bool selected) const;
+// kRewrites lets the clean_tombstones pass empty the buckets it takes out.
+template <class F>
+struct FunctorSel {
+  F f;
+  static constexpr bool kRewrites = false;
+  template <class T>
+  __device__ __forceinline__ bool operator()(const T& x) const {
+    return f(x);
+  }
+  template <class T>
+  __device__ __forceinline__ void rewrite(T*, uint64_t, const T&, bool) const {}
+};
+struct ScanSel {  // placeholder selector of the scan
+  static constexpr bool kRewrites = false;
+  template <class T>
+  __device__ __forceinline__ bool operator()(const T&) const {
+    return true;
+  }
+  template <class T>
+  __device__ __forceinline__ void rewrite(T*, uint64_t, const T&, bool) const {}
+};
+
+struct Done {                              // what the pass reports, and where it starts
+  unsigned long long* d_count;              // if set, *d_count = min(total, count_max) (compaction)
+  unsigned long long* sub_from;             // if set, *sub_from -= total (clean_tombstones' fill)
+  const unsigned* skip;                     // if set and *skip != 0, the pass does nothing at all
+  unsigned long long count_max = ~0ull;     // the largest count written to *d_count
+  const unsigned long long* base_from = nullptr;  // if set, output starts at out[*base_from] (and
+                                                  // the total counts it), after elements placed earlier
+  const unsigned long long* n_from = nullptr;     // if set, the input has min(n, *n_from) elements,
+                                                  // read on the device (n is then an upper bound)
+};
+
+// ---------------------------------------------------------------------------
+// The kernel. SCAN: T = O = uint32_t, out[i] = sum of in[0..i) mod 2^32.
+// Otherwise: out[0..c) = the selected elements (projected to O) in input
+// order, writes beyond `capacity` dropped, c to *done.d_count.
+// ---------------------------------------------------------------------------
+template <class T, class O, class Sel, bool SCAN>
+__global__ void __launch_bounds__(kBlock) k_stream(const T* __restrict__ in, O* __restrict__ out, uint64_t n,
+                                                  Sel sel, uint64_t capacity, Done done, Scratch sc) {
+  constexpr int E = 16 / sizeof(T);
+  constexpr int WARPS = kBlock / 32;
+  constexpr unsigned SU4 = kBlock * kR;  // uint4 per slice
+  constexpr unsigned SE = SU4 * E;       // elements per slice
+  static_assert(!SCAN || std::is_same<T, uint32_t>::value, "the scan is over uint32_t");
+  static_assert(sizeof(O) <= sizeof(T), "the packed result fits in its stage");
+  extern __shared__ __align__(128) uint4 s_stage[];  // kStages x SU4
+  __shared__ __align__(8) uint64_t s_bar[kStages];
+  __shared__ unsigned s_warp[WARPS];
+  __shared__ unsigned s_cnt[kStages];
+  __shared__ unsigned long long s_red[2][WARPS];
+  __shared__ int s_abort;
+
+  // Device-side inputs: the same values for every CTA, so every CTA runs the
+  // same phases and none waits on a CTA that skipped.
+  if (done.skip && *done.skip) return;
+  if (done.n_from && *done.n_from < n) n = *done.n_from;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned G = gridDim.x, b = blockIdx.x;
+  const uint64_t full_slices = n / SE;  // slices wholly inside [0, n)
+  const unsigned long long phases = ((n + SE - 1) / SE + G - 1) / G;
+  unsigned pend = 0;                    // thread 0: stages with a bulk copy not yet seen complete
+  unsigned par = 0;                     // parity of the next wait, bit per stage
+
+  // Fill stage st with the slice of phase p (thread 0): a whole slice by one
+  // bulk copy; the ragged last slice and slices past n are read later with
+  // plain loads, so their barrier phase completes with no bytes.
+  auto issue = [&](int st, unsigned long long p) {
+    const uint64_t t = p * G + b;
+    if (t < full_slices) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier reads of the stage come first
+      mbar_expect_tx(&s_bar[st], kSliceBytes);
+      bulk_load(s_stage + (size_t)st * SU4, in + t * SE, kSliceBytes, &s_bar[st]);
+    } else {
+      mbar_expect_tx(&s_bar[st], 0);
+    }
+    pend |= 1u << st;
+  };
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) mbar_init(&s_bar[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_abort = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int s = 0; s < kStages && (unsigned long long)s < phases; ++s) issue(s, s);
+
+  // result count (or sum) of the phases already written, after any elements placed before this pass
+  unsigned long long base = done.base_from ? *done.base_from : 0ull;
+  bool failed = false;
+  for (unsigned long long p = 0; p < phases + kDefer; ++p) {
+    // ---- pass 1: phase p -------------------------------------------------
+    if (p < phases) {
+      const int st = (int)(p % kStages);
+      const bool ok = mbar_wait(&s_bar[st], (par >> st) & 1u);
+      if (ok) {  // a failed wait leaves par and pend as they were, for the drain below
+        par ^= 1u << st;
+        pend &= ~(1u << st);
+      }
+      const uint64_t t = p * G + b;
+      const bool whole = t < full_slices;
+      const uint64_t e0 = t * SE;
+      T x[kR][E];
+      uint4* stage = s_stage + (size_t)st * SU4;
+      const unsigned wbase = warp * 32 * kR;  // this warp's first uint4 of the slice
+#pragma unroll
+      for (int r = 0; r < kR; ++r) {
+        const unsigned u = wbase + r * 32 + lane;
+        if (whole) {
+          const uint4 q = stage[u];
+          memcpy(&x[r][0], &q, 16);
+        } else {
+#pragma unroll
+          for (int q = 0; q < E; ++q) {
+            const uint64_t e = e0 + (uint64_t)u * E + q;
+            if (e < n) x[r][q] = in[e];
+            else memset(&x[r][q], 0, sizeof(T));
+          }
+        }
+      }
+      if (__syncthreads_or(!ok)) {  // stage st is read; a failed wait stops every thread here
+        failed = true;
+        break;
+      }
+      unsigned pre[kR];
+      unsigned acc = 0;
+      unsigned bits[kR];
+#pragma unroll
+      for (int r = 0; r < kR; ++r) {
+        unsigned c;
+        if constexpr (SCAN) {
+          c = x[r][0] + x[r][1] + x[r][2] + x[r][3];
+          bits[r] = 0;
+        } else {
+          const uint64_t e = e0 + (uint64_t)(wbase + r * 32 + lane) * E;
+          unsigned m = 0;
+#pragma unroll
+          for (int q = 0; q < E; ++q) {
+            const bool in_range = whole || e + q < n;
+            const bool s = in_range && sel(x[r][q]);
+            if (s) m |= 1u << q;
+            if constexpr (Sel::kRewrites) {
+              if (in_range) sel.rewrite(const_cast<T*>(in), e + q, x[r][q], s);
+            }
+          }
+          bits[r] = m;
+          c = __popc(m);
+        }
+        const unsigned incl = warp_incl_scan(c, lane);
+        pre[r] = acc + incl - c;
+        acc += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      if (lane == 0) s_warp[warp] = acc;
+      __syncthreads();
+      if (warp == 0) {
+        const unsigned wt = lane < WARPS ? s_warp[lane] : 0u;
+        const unsigned wincl = warp_incl_scan(wt, lane);
+        if (lane < WARPS) s_warp[lane] = wincl - wt;
+        if (lane == 31) {
+          s_cnt[st] = wincl;
+          // publish this CTA's count (or sum, mod 2^32) of phase p, tagged with p + 1
+          st_relaxed(sc.slots + (p % kSlots) * G + b, ((p + 1) << 32) | wincl);
+        }
+      }
+      __syncthreads();
+      // the CTA-local result, in place in the stage (every thread has read it)
+      const unsigned woff = s_warp[warp];
+      if constexpr (SCAN) {
+#pragma unroll
+        for (int r = 0; r < kR; ++r) {
+          const unsigned o0 = woff + pre[r], o1 = o0 + x[r][0], o2 = o1 + x[r][1], o3 = o2 + x[r][2];
+          stage[wbase + r * 32 + lane] = make_uint4(o0, o1, o2, o3);
+        }
+      } else {
+        O* packed = reinterpret_cast<O*>(stage);
+#pragma unroll
+        for (int r = 0; r < kR; ++r) {
+          unsigned o = woff + pre[r];
+#pragma unroll
+          for (int q = 0; q < E; ++q)
+            if (bits[r] & (1u << q)) packed[o++] = hxs::project<T, O>(x[r][q]);
+        }
+      }
+    }
+    // ---- pass 2: phase p - D ---------------------------------------------
+    if (p >= (unsigned long long)kDefer) {
+      const unsigned long long q = p - kDefer;
+      const int st = (int)(q % kStages);
+      // every CTA's count of phase q: the sum over CTAs before this one, and the total
+      unsigned long long before = 0, total = 0;
+      bool ok = true;
+      for (unsigned c = threadIdx.x; c < G; c += kBlock) {
+        const unsigned long long* slot = sc.slots + (q % kSlots) * G + c;
+        unsigned long long v = ld_relaxed(slot);
+        if ((v >> 32) != q + 1) {
+          const unsigned long long t0 = globaltimer();
+          unsigned i = 0;
+          while ((v >> 32) != q + 1) {
+            if ((++i & 63) == 0) {
+              if (ld_relaxed_u32(sc.error) || globaltimer() - t0 > kWaitNs) {
+                ok = false;
+                break;
+              }
+              __nanosleep(64);
+            }
+            v = ld_relaxed(slot);
+          }
+          if (!ok) break;
+        }
+        const unsigned long long cnt = v & 0xffffffffull;
+        total += cnt;
+        if (c < b) before += cnt;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        before += __shfl_xor_sync(0xffffffffu, before, o);
+        total += __shfl_xor_sync(0xffffffffu, total, o);
+      }
+      if (lane == 0) {
+        s_red[0][warp] = before;
+        s_red[1][warp] = total;
+      }
+      if (__syncthreads_or(!ok)) {
+        failed = true;
+        break;
+      }
+      before = 0;
+      total = 0;
+#pragma unroll
+      for (int w = 0; w < WARPS; ++w) {
+        before += s_red[0][w];
+        total += s_red[1][w];
+      }
+      const unsigned long long prefix = base + before;
+      const uint4* stage = s_stage + (size_t)st * SU4;
+      const uint64_t t = q * G + b;
+      if constexpr (SCAN) {
+        const uint64_t e0 = t * SE;
+        const unsigned add = (unsigned)prefix;
+        const bool whole = t < full_slices;
+        uint32_t* o32 = reinterpret_cast<uint32_t*>(out);
+        for (unsigned u = threadIdx.x; u < SU4; u += kBlock) {
+          const uint4 v = stage[u];
+          const uint4 w = make_uint4(v.x + add, v.y + add, v.z + add, v.w + add);
+          const uint64_t e = e0 + (uint64_t)u * 4;
+          if (whole) {
+            __stcs(reinterpret_cast<uint4*>(o32 + e), w);
+          } else {
+            const unsigned a[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+              if (e + k < n) o32[e + k] = a[k];
+          }
+        }
+      } else {
+        const O* packed = reinterpret_cast<const O*>(stage);
+        const unsigned cnt = s_cnt[st];
+        for (unsigned i = threadIdx.x; i < cnt; i += kBlock) {
+          const unsigned long long dst = prefix + i;
+          if (dst < capacity) out[dst] = packed[i];
+        }
+      }
+      base += total;
+      __syncthreads();  // stage st is written out
+      if (threadIdx.x == 0 && q + kStages < phases) issue(st, q + kStages);
+    }
+  }
+  if (failed) {
+    if (threadIdx.x == 0) {
+      atomicExch(sc.error, 1u);
+      // no copy is issued after a failure: give each one still in flight a
+      // bounded wait before the CTA exits
+      for (int s = 0; s < kStages; ++s)
+        if ((pend >> s) & 1u) mbar_wait(&s_bar[s], (par >> s) & 1u);
+    }
+    return;
+  }
+  if (b == 0 && threadIdx.x == 0) {
+    if (done.d_count) *done.d_count = base < done.count_max ? base : done.count_max;
+    if (done.sub_from) atomicAdd(done.sub_from, 0ull - base);
+  }
+}
+
+// ---- host side -------------------------------------------------------------
+inline size_t smem_bytes() { return (size_t)kStages * kSliceBytes; }
+
+// Co-resident CTAs of one instantiation on the current device (SMs x CTAs
+// per SM, at most kMaxGrid), queried once per instantiation and device.
+template <class T, class O, class Sel, bool SCAN>
+inline cudaError_t resident_grid(unsigned* grid) {
+  auto kern = k_stream<T, O, Sel, SCAN>;
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  int g = (dev >= 0 && dev < 64) ? cache[dev].load(std::memory_order_relaxed) : 0;
+  if (g == 0) {
+    const size_t smem = smem_bytes();
+    if (smem > 48 * 1024) {
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    int per_sm = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, smem);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    g = per_sm * sms;
+    if (g < 1) return cudaErrorInvalidConfiguration;
+    if (g > kMaxGrid) g = kMaxGrid;
+    if (dev >= 0 && dev < 64) cache[dev].store(g, std::memory_order_relaxed);  // every writer stores the same
+  }
+  *grid = (unsigned)g;
+  return cudaSuccess;
+}
+
+// Launches one pass over n > 0 elements of a 16-byte-aligned `in` (and, for
+// the scan, a 16-byte-aligned `out`). scratch: scratch_need(n, sizeof(T))
+// bytes of device memory; the part this launch uses is zeroed here, on the
+// stream. With done.n_from, n is an upper bound of the device-side count.
+template <class T, class O, class Sel, bool SCAN>
+inline cudaError_t launch(const T* in, O* out, uint64_t n, const Sel& sel, uint64_t capacity, Done done,
+                          void* scratch, cudaStream_t s) {
+  auto kern = k_stream<T, O, Sel, SCAN>;
+  unsigned grid = 0;
+  cudaError_t e = resident_grid<T, O, Sel, SCAN>(&grid);
+  if (e != cudaSuccess) return e;
+  constexpr uint64_t SE = (uint64_t)kBlock * kR * (16 / sizeof(T));
+  const uint64_t slices = (n + SE - 1) / SE;
+  if (slices < grid) grid = (unsigned)slices;
+  e = cudaMemsetAsync(scratch, 0, scratch_bytes_used(grid), s);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kBlock);
+  cfg.dynamicSmemBytes = smem_bytes();
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, in, out, n, sel, capacity, done, carve(scratch));
+}
+
+}  // namespace hxs

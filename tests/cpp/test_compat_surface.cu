@@ -112,6 +112,7 @@ static void test_arena_and_key_overloads() {
   k4.reserve(N);
   split::tools::copy_if_loop(src, o3, Predicate());
   split::tools::copy_if_keys_loop(src, k4, Predicate());
+  cudaDeviceSynchronize();
   EXPECT_TRUE(o3.size() == N / 2 && k4.size() == N / 2);
   ok = true;
   for (size_t i = 0; i < o3.size() && i < k4.size() && i < o1.size(); ++i) ok = ok && o3[i] == o1[i] && k4[i] == 2 * i;
@@ -150,12 +151,15 @@ static void test_more_host_methods() {
   auto odd_valid = [] __host__ __device__(hash_pair<key_type, val_type> & e) -> bool {
     return e.first != 0xFFFFFFFFu && e.first != 0xFFFFFFFEu && e.second % 2 == 1;
   };
-  vector e1, e2;
-  split::SplitVector<key_type> k1, k2;
+  // the loop forms write into the output's capacity (the reference's
+  // loop_compact asserts that it suffices), so the outputs are sized first
+  vector e1(N), e2(N);
+  split::SplitVector<key_type> k1(N), k2(N);
   b.extractLoop(e1);
   b.extractPatternLoop(e2, odd_valid);
   b.extractAllKeysLoop(k1);
   b.extractKeysByPatternLoop(k2, odd_valid);
+  cudaDeviceSynchronize();  // the loop forms set the sizes on the device, without a host synchronisation
   EXPECT_TRUE(e1.size() == N / 2 && e2.size() == N / 2 && k1.size() == N / 2 && k2.size() == N / 2);
   bool ok = true;
   for (auto& e : e1) ok = ok && e.first % 2 == 1 && e.second == e.first;

@@ -12,6 +12,7 @@ def declared_symbols():
     for h in (ROOT / "include").glob("*.h"):
         text = h.read_text()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"^\s*typedef[^;]*;", "", text, flags=re.M)  # function-pointer types are not entry points
         for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(hx_[a-z0-9_]+)\s*\(", text, flags=re.M):
             syms.add(m.group(1))
     return sorted(syms)
@@ -81,8 +82,11 @@ def test_null_handles_and_outputs_are_rejected(hx):
 
 
 def test_scratch_sizes_and_undersized_caller_scratch(hx):
-    """hx_scratch_bytes: the scan needs a 256-byte header and one 8-byte status per 4096-element tile; copy_if
-    needs at least as much plus a 256-byte count area, never shrinking as n grows. A caller buffer smaller than
+    """hx_scratch_bytes: the scan needs the larger of its two kernels' scratch — a 256-byte header and one
+    8-byte status per 12288-element tile (buffers that are not 16-byte aligned), or a 256-byte header and
+    2 * 2 + 2 count slots of 8 bytes for each CTA, at most one CTA per 4096-element slice and 2048 CTAs (the
+    phase-partitioned kernel); copy_if needs at least as much plus a 256-byte count area, never shrinking as
+    n grows. A caller buffer smaller than
     the need is rejected before any device work: every call here is one that must be rejected, so the fake
     pointers are never dereferenced."""
     lib = hx.lib()
@@ -93,7 +97,8 @@ def test_scratch_sizes_and_undersized_caller_scratch(hx):
         return b.value
 
     for n in (0, 1, 4095, 4096, 4097, 1 << 20, (1 << 28) + 3):
-        assert need(hx.SCRATCH_SCAN, n) == 256 + 8 * max(1, -(-n // 4096))
+        assert need(hx.SCRATCH_SCAN, n) == max(256 + 8 * max(1, -(-n // 12288)),
+                                               256 + 8 * 6 * min(2048, max(1, -(-n // 4096))))
     prev = 0
     for n in (0, 1, 100, 5000, 1 << 16, 1 << 20, 1 << 24):
         c = need(hx.SCRATCH_COPY_IF, n)

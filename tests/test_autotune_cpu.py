@@ -1,84 +1,40 @@
-"""Host logic of the batched-maps autotuner, without a GPU: a fake plan whose
-run time depends on its tuning and a fake CUDA event clock. The tuner tries
-every point of the grid, resets the maps before every trial, times `reps`
-trials after one warm-up, and leaves the plan on the fastest setting."""
+"""Host logic of libhx's batched-maps autotuner, without a GPU: the search
+behind hx_batch_autotune (hashinator_gb300/csrc/hx_autotune.h) compiled into
+a C++ host program (tests/cpp/test_autotune_host.cpp) that drives it with a
+fake plan and a fake clock."""
+import shutil
+import subprocess
+from pathlib import Path
+
 import pytest
 
-from hashinator_gb300 import autotune
+ROOT = Path(__file__).resolve().parents[1]
 
 
-class FakeClock:
-    now = 0.0
+def test_autotune_search_on_the_host(tmp_path):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    exe = tmp_path / "test_autotune_host"
+    r = subprocess.run([cxx, "-std=c++17", "-O1", "-Wall", "-Werror", "-I", str(ROOT / "hashinator_gb300" / "csrc"),
+                        str(ROOT / "tests" / "cpp" / "test_autotune_host.cpp"), "-o", str(exe)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-3000:]
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "PASSED" in r.stdout, r.stdout[-2000:]
 
 
-class FakeEvent:
-    def __init__(self, enable_timing=False):
-        self.t = None
+def test_python_caller_passes_the_grid_and_reports_the_best():
+    """autotune_batch forwards its grid and reset to BatchPlan.autotune and shapes the result."""
+    from hashinator_gb300 import autotune
 
-    def record(self, stream=None):
-        self.t = FakeClock.now
+    class Plan:
+        def autotune(self, groups, blocks, tiles, reps, reset, stream):
+            self.args = (groups, blocks, tiles, reps, reset, stream)
+            return (8, 256, 2048, 1.25), [(1, 128, 512, 3.0), (8, 256, 2048, 1.25)]
 
-    def synchronize(self):
-        pass
-
-    def elapsed_time(self, other):
-        return other.t - self.t
-
-
-class FakePlan:
-    def __init__(self, cost):
-        self.cost = cost
-        self.tuning = None
-        self.history = []
-        self.runs = 0
-
-    def set_tuning(self, g, b, t, stream=None):
-        self.tuning = (g, b, t)
-        self.history.append(self.tuning)
-
-    def run(self, stream=None):
-        self.runs += 1
-        # the first run of each setting is slow (warm-up), later ones cost the model's time
-        FakeClock.now += self.cost(*self.tuning) + (5.0 if self.first else 0.0)
-        self.first = False
-
-
-@pytest.fixture
-def fake_cuda(monkeypatch):
-    torch = pytest.importorskip("torch")
-    monkeypatch.setattr(torch.cuda, "Event", FakeEvent)
-    return torch
-
-
-def test_picks_the_fastest_setting_and_leaves_the_plan_on_it(fake_cuda):
-    def cost(g, b, t):
-        return 1.0 + abs(g - 8) * 0.1 + abs(b - 256) / 1000 + abs(t - 2048) / 10000
-
-    plan = FakePlan(cost)
-    resets = []
-
-    class Hook:
-        def __call__(self):
-            resets.append(plan.tuning)
-            plan.first = len(resets) == 1 or resets[-1] != resets[-2]
-
-    res = autotune.autotune_batch(plan, Hook(), groups=(1, 4, 8, 16), blocks=(128, 256, 512),
-                                  tiles=(512, 2048, 8192), reps=2, stream=object())
-    assert res["best"] == (8, 256, 2048)
-    assert plan.tuning == (8, 256, 2048)  # left on the winner
-    assert len(res["trials"]) == 4 * 3 * 3
-    assert plan.runs == 4 * 3 * 3 * 3  # warm-up + 2 timed runs per setting
-    assert len(resets) == plan.runs + 1  # before every run, and once more at the end
-    best = min(res["trials"], key=lambda r: r["ms"])
-    assert (best["group"], best["block"], best["tile"]) == res["best"]
-    assert res["ms"] == pytest.approx(cost(8, 256, 2048))  # warm-up excluded from the timing
-
-
-def test_single_point_grid(fake_cuda):
-    plan = FakePlan(lambda g, b, t: 2.5)
-
-    def reset():
-        plan.first = False
-
-    res = autotune.autotune_batch(plan, reset, groups=(1,), blocks=(128,), tiles=(2048,), reps=3, stream=object())
-    assert res["best"] == (1, 128, 2048) and res["ms"] == pytest.approx(2.5) and len(res["trials"]) == 1
+    p = Plan()
+    res = autotune.autotune_batch(p, None, groups=(1, 8), blocks=(128, 256), tiles=(512, 2048), reps=3, stream="s")
+    assert p.args == ((1, 8), (128, 256), (512, 2048), 3, None, "s")
+    assert res["best"] == (8, 256, 2048) and res["ms"] == 1.25 and len(res["trials"]) == 2
+    assert res["trials"][1] == {"group": 8, "block": 256, "tile": 2048, "ms": 1.25}

@@ -27,7 +27,8 @@ def _compile(src: Path, out: Path, lambdas: bool = True):
 
 
 @pytest.mark.parametrize("name,lambdas", [("test_compat", True), ("test_compat_device", True),
-                                          ("test_device_api", False), ("test_compat_surface", True)])
+                                          ("test_device_api", False), ("test_compat_surface", True),
+                                          ("test_splitvector_device", True)])
 def test_cpp_sources_compile_against_the_header(tmp_path, name, lambdas):
     r = _compile(ROOT / "tests" / "cpp" / f"{name}.cu", tmp_path / f"{name}.o", lambdas)
     assert r.returncode == 0, r.stderr[-3000:]

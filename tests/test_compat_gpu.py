@@ -47,3 +47,19 @@ def test_reference_device_api_tests_through_compat_header(hx, tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
     print(r.stdout[-4000:], r.stderr[-2000:])
     assert r.returncode == 0 and "PASSED" in r.stdout
+
+
+def test_splitvector_device_surface_and_caller_scratch(hx, tmp_path):
+    """The SplitVector device surface (upload, device_push_back, device_resize, device_insert) with the
+    reference's own device tests and a concurrent device_push_back checked against a host model; the
+    preallocated compactions from several host threads and streams with caller scratch and no stream-ordered
+    allocation; copy_if_loop reading a device-side size; functor copy_if equal to libhx's descriptor copy_if."""
+    from hashinator_gb300 import build
+    exe = tmp_path / "test_splitvector_device"
+    cmd = [build._nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17", "--extended-lambda",
+           "-I", str(ROOT / "include"), str(ROOT / "tests" / "cpp" / "test_splitvector_device.cu"), "-o", str(exe),
+           "-L", str(hx.LIB_PATH.parent), "-lhx", f"-Xlinker=-rpath,{hx.LIB_PATH.parent}"]
+    subprocess.run(cmd, check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
+    print(r.stdout[-4000:], r.stderr[-2000:])
+    assert r.returncode == 0 and "PASSED" in r.stdout
