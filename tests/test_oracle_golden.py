@@ -63,3 +63,48 @@ def test_oracle_clean_and_rehash_keep_mapping(oracle_mod, name):
     k, v = m.mapping()
     np.testing.assert_array_equal(k, g["map_keys"])
     np.testing.assert_array_equal(v, g["map_vals"])
+
+
+class _OracleAdapter:
+    def __init__(self, oracle_mod, sp, kb):
+        self.m = oracle_mod.OracleMap(sp, kb)
+        self.sp = sp
+
+    def insert(self, k, v):
+        assert self.m.insert(k, v, target_lf=0.0) == 0
+
+    def retrieve(self, q, out):
+        self.m.retrieve(q, out)
+
+    def erase(self, k):
+        self.m.erase(k)
+
+    def clean(self, sp):
+        if sp == self.sp:
+            self.m.clean_tombstones()
+        else:
+            self.m.resize(sp)
+            self.sp = sp
+
+    def fill(self):
+        return self.m.info()["fill"]
+
+    def mapping(self):
+        return self.m.mapping()
+
+
+@pytest.mark.parametrize("name", __import__("golden_replay").seq_cases())
+def test_oracle_matches_reference_sequences(oracle_mod, name):
+    """Insert after erase, upserts of present keys, clean (the reference's resize) then inserts: every size,
+    query output and the final mapping equal the reference's CPU build."""
+    import golden_replay
+    g = golden_replay.load_seq(name)
+    golden_replay.replay(g, _OracleAdapter(oracle_mod, int(g["size_power"]), int(g["key_bytes"])))
+
+
+def test_oracle_matches_reference_full_size_plain_map(oracle_mod):
+    """The plain single-map workload at its full size (2^20 keys, 2^21 buckets), through the digests of the
+    reference's outputs."""
+    import golden_replay
+    d = golden_replay.cfg1_expected()
+    golden_replay.check_cfg1(_OracleAdapter(oracle_mod, d["size_power"], 4), d)
