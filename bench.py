@@ -1085,14 +1085,42 @@ def run_ours(args):
 
 
 def run_case(args):
-    """One hash-kernel case on its own, for an ncu capture: a table of 2^case_log_buckets buckets, the
-    case_lf share of them inserted (case_reps times, each after a clear), then the same number of 50%-hit
-    queries (case_reps times). Prints one JSON line with the per-launch times."""
+    """One kernel case on its own, for an ncu capture. --case-kind map: a table of 2^case_log_buckets buckets,
+    the case_lf share of them inserted (case_reps times, each after a clear), then the same number of 50%-hit
+    queries (case_reps times). --case-kind copy_if / scan: 2^case_log_n uniform u32, copy_if with
+    (x % 100) < case_s, or the exclusive scan of x & 15, case_reps times. Prints one JSON line with the
+    per-launch times."""
     import torch
     import hashinator_gb300 as hx
     from hashinator_gb300 import workloads
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
+    if args.case_kind != "map":
+        n = 1 << args.case_log_n
+        g = torch.Generator(device=dev).manual_seed(7)
+        x = torch.randint(0, 2**31 - 1, (n,), dtype=torch.int64, device=dev, generator=g)
+        x = (x * 2 + (x >> 17 & 1)).to(torch.int32)
+        out = torch.empty_like(x)
+        stream = torch.cuda.Stream(device=dev)
+        if args.case_kind == "copy_if":
+            nb = hx.tools.scratch_bytes(hx.SCRATCH_COPY_IF, n)
+            sc = torch.empty(nb, dtype=torch.uint8, device=dev)
+            dc = torch.zeros(1, dtype=torch.int64, device=dev)
+            t = _ev_time(stream, lambda: hx.tools.copy_if(x, out, hx.Pred.mod_lt(100, args.case_s), scratch=sc,
+                                                          scratch_bytes=nb, stream=stream, d_count=dc),
+                         reps=args.case_reps)
+            c = int(dc.item())
+            nbytes = 4 * n + 4 * c
+        else:
+            y = (x & 15).contiguous()
+            nb = hx.tools.scratch_bytes(hx.SCRATCH_SCAN, n)
+            sc = torch.empty(nb, dtype=torch.uint8, device=dev)
+            t = _ev_time(stream, lambda: hx.tools.split_prefix_scan(y, out, scratch=sc, scratch_bytes=nb,
+                                                                    stream=stream), reps=args.case_reps)
+            nbytes = 8 * n
+        print(json.dumps({"case": f"{args.case_kind} 2^{args.case_log_n} u32", "ms": round(t * 1e3, 4),
+                          "GB_s": round(nbytes / t / 1e9, 1)}), flush=True)
+        return 0
     w, sp = args.case_key_bytes, args.case_log_buckets
     n = int(args.case_lf * (1 << sp))
     keys, vals, q, _ = workloads.large_map_workload(n, w, 31 + w)
@@ -1138,6 +1166,9 @@ def main():
     ap.add_argument("--case-lf", type=float, default=0.5)
     ap.add_argument("--case-log-buckets", type=int, default=27)
     ap.add_argument("--case-reps", type=int, default=1)
+    ap.add_argument("--case-kind", default="map", choices=["map", "copy_if", "scan"])
+    ap.add_argument("--case-log-n", type=int, default=26)
+    ap.add_argument("--case-s", type=int, default=1, help="copy_if selectivity in percent")
     args = ap.parse_args()
     if args.case:
         return run_case(args)

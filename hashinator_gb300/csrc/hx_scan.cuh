@@ -229,7 +229,17 @@ __global__ void __launch_bounds__(BLOCK) k_scan_u32(const uint32_t* in, uint32_t
 // Predicate kinds compiled into the compaction kernel; the launch picks one
 // from hx_pred.op, so the hot rules cost a few instructions per element
 // instead of a switch (and a division) per element.
-enum : int { PK_GENERIC = 0, PK_MOD_LT32 = 1, PK_MASK_EQ = 2, PK_VALID = 3 };
+enum : int { PK_GENERIC = 0, PK_MOD_LT32 = 1, PK_MASK_EQ = 2, PK_VALID = 3, PK_MOD_LT_THRESH = 4 };
+
+// (x mod d) < s for 32-bit x and 2 <= d <= 2^31, 0 < s < d, with one 64-bit
+// multiply and a compare, derived from the direct-remainder method cited
+// below: with M = ceil(2^64 / d), write x = q*d + r and M*d = 2^64 + e
+// (0 <= e < d); then M*x mod 2^64 = r*M + q*e without wrapping, and because
+// q*e < 2^32 < M, r < s exactly when M*x mod 2^64 < s*M. The host computes
+// the threshold s*M (below 2^64, as s < d).
+__host__ __device__ inline bool mod_lt_thresh_ok(uint64_t d, uint64_t s) {
+  return d >= 2 && d <= (1ull << 31) && s > 0 && s < d;
+}
 
 // x mod d for 32-bit x and 1 <= d < 2^32 by direct computation (D. Lemire,
 // O. Kaser, N. Kurz, "Faster Remainder by Direct Computation: Applications to
@@ -552,9 +562,22 @@ struct PredSel {
   hx_pred pr;
   uint64_t magic;
   typename ElemOps<T>::Ctx ctx;
+  uint64_t thresh = 0;  // PK_MOD_LT_THRESH: s * magic
   static constexpr bool kRewrites = CLEAN;
   __device__ __forceinline__ bool operator()(const T& x) const {
-    return ElemOps<T>::template pred<PK>(pr, x, ctx, magic);
+    if constexpr (PK == PK_MOD_LT_THRESH) {
+      uint32_t f;
+      if constexpr (std::is_same<T, uint32_t>::value) f = x;
+      else f = (uint32_t)(pr.field == HX_FIELD_VALUE ? x.second : x.first);
+      bool r = magic * (uint64_t)f < thresh;
+      if constexpr (!std::is_same<T, uint32_t>::value) {
+        using Tr = PairTraits<T>;
+        if ((pr.flags & HX_PRED_SKIP_SENTINELS) && (x.first == Tr::EMPTY || x.first == Tr::TOMB)) r = false;
+      }
+      return (pr.flags & HX_PRED_NEGATE) ? !r : r;
+    } else {
+      return ElemOps<T>::template pred<PK>(pr, x, ctx, magic);
+    }
   }
   __device__ __forceinline__ void rewrite(T* in, uint64_t i, const T& x, bool selected) const {
     if constexpr (CLEAN) {
@@ -588,6 +611,10 @@ inline cudaError_t launch_compact(const T* in, O* out, uint64_t n, const hx_pred
     } else {
       switch (pred_kind<T>(pr)) {
         case PK_MOD_LT32:
+          if (mod_lt_thresh_ok(pr.a, pr.b)) {
+            const uint64_t m = fastmod_magic((uint32_t)pr.a);
+            return go(PredSel<T, PK_MOD_LT_THRESH, false>{pr, m, ctx, pr.b * m});
+          }
           return go(PredSel<T, PK_MOD_LT32, false>{pr, fastmod_magic((uint32_t)pr.a), ctx});
         case PK_MASK_EQ:
           return go(PredSel<T, PK_MASK_EQ, false>{pr, 0, ctx});

@@ -121,6 +121,7 @@ static_assert(kDefer >= 1 && kDefer < kStages, "a stage must be free to load whi
 // after every CTA has read it (see the kernel), which needs 2 * D + 2 slots.
 constexpr int kSlots = 2 * kDefer + 2;
 constexpr int kMaxGrid = 2048;
+constexpr int kSlotLoads = kMaxGrid / kBlock;  // count slots each thread reads per phase
 constexpr unsigned kSliceBytes = kBlock * kR * 16;
 
 // Scratch: [error word u32][pad .. 256 B][count slots u64 x kSlots x grid].
@@ -250,6 +251,17 @@ __global__ void __launch_bounds__(kBlock) k_stream(const T* __restrict__ in, O* 
   unsigned long long base = done.base_from ? *done.base_from : 0ull;
   bool failed = false;
   for (unsigned long long p = 0; p < phases + kDefer; ++p) {
+    // The count slots that pass 2 reads below were published kDefer phases
+    // ago: load them now, so that their latency overlaps pass 1.
+    unsigned long long pv[kSlotLoads];
+    if (p >= (unsigned long long)kDefer) {
+      const unsigned long long* row = sc.slots + ((p - kDefer) % kSlots) * G;
+#pragma unroll
+      for (int k = 0; k < kSlotLoads; ++k) {
+        const unsigned c = threadIdx.x + k * kBlock;
+        pv[k] = c < G ? ld_relaxed(row + c) : 0ull;
+      }
+    }
     // ---- pass 1: phase p -------------------------------------------------
     if (p < phases) {
       const int st = (int)(p % kStages);
@@ -350,9 +362,12 @@ __global__ void __launch_bounds__(kBlock) k_stream(const T* __restrict__ in, O* 
       // every CTA's count of phase q: the sum over CTAs before this one, and the total
       unsigned long long before = 0, total = 0;
       bool ok = true;
-      for (unsigned c = threadIdx.x; c < G; c += kBlock) {
+#pragma unroll
+      for (int k = 0; k < kSlotLoads; ++k) {
+        const unsigned c = threadIdx.x + k * kBlock;
+        if (c >= G) break;
         const unsigned long long* slot = sc.slots + (q % kSlots) * G + c;
-        unsigned long long v = ld_relaxed(slot);
+        unsigned long long v = pv[k];
         if ((v >> 32) != q + 1) {
           const unsigned long long t0 = globaltimer();
           unsigned i = 0;

@@ -2,8 +2,10 @@
 with Python integers: the direct-remainder method used by the compaction's
 `x % d < s` predicate (hx_scan.cuh fastmod_magic / fastmod_u32: with
 M = floor((2^64 - 1) / d) + 1 mod 2^64, x mod d is the high 64 bits of
-((M * x) mod 2^64) * d, for 32-bit x and 1 <= d < 2^32), and the build
-flags (sm_103a only, with line info)."""
+((M * x) mod 2^64) * d, for 32-bit x and 1 <= d < 2^32), the one-multiply
+threshold form of `x % d < s` (hx_scan.cuh PK_MOD_LT_THRESH: for 2 <= d <=
+2^31 and 0 < s < d, (x mod d) < s exactly when (M * x) mod 2^64 < s * M), and
+the build flags (sm_103a only, with line info)."""
 import random
 
 import pytest
@@ -37,6 +39,45 @@ def test_direct_remainder_random_divisors():
         for _ in range(50):
             x = rng.randrange(1 << 32)
             assert fastmod(x, d) == x % d, (x, d)
+
+
+def thresh_ok(d: int, s: int) -> bool:  # mod_lt_thresh_ok in hx_scan.cuh
+    return 2 <= d <= (1 << 31) and 0 < s < d
+
+
+def mod_lt_by_threshold(x: int, d: int, s: int) -> bool:
+    magic = (M64 // d + 1) & M64
+    t = s * magic
+    assert t <= M64  # the threshold fits 64 bits
+    return ((magic * x) & M64) < t
+
+
+@pytest.mark.parametrize("d", [d for d in DIVISORS if 2 <= d <= (1 << 31)])
+def test_threshold_form_matches_modulo(d):
+    rng = random.Random(d + 1)
+    ss = sorted({1, 2, d // 2, d - 1} | {rng.randrange(1, d) for _ in range(5)})
+    xs = [0, 1, d - 1, d, d + 1, 2 * d - 1, (1 << 32) - 1, (1 << 32) - 2, (1 << 31), (1 << 31) - 1]
+    xs += [rng.randrange(1 << 32) for _ in range(1500)]
+    xs += [k * d + r for k in (0, 1, rng.randrange(1, (1 << 32) // d)) for r in (0, 1, d - 1) if k * d + r < (1 << 32)]
+    for s in ss:
+        if not thresh_ok(d, s):
+            continue
+        for x in xs:
+            if x < (1 << 32):
+                assert mod_lt_by_threshold(x, d, s) == (x % d < s), (x, d, s)
+
+
+def test_threshold_form_random_divisors_and_its_limit():
+    rng = random.Random(11)
+    for _ in range(300):
+        d = rng.randrange(2, (1 << 31) + 1)
+        s = rng.randrange(1, d)
+        for _ in range(40):
+            x = rng.randrange(1 << 32)
+            assert mod_lt_by_threshold(x, d, s) == (x % d < s), (x, d, s)
+    # the argument that the form is exact (q * e < 2^32 < M and no wrap of r*M + q*e) needs d <= 2^31: larger
+    # divisors, and s = 0 or s >= d, use the direct remainder instead
+    assert not thresh_ok((1 << 31) + 1, 5) and not thresh_ok(100, 0) and not thresh_ok(100, 100)
 
 
 def test_build_targets_sm103a_with_line_info():
