@@ -122,9 +122,9 @@ __global__ void k_fill(T* p, size_t n, T v) {
  * object, and device_push_back / device_resize / device_insert change the
  * size that the host reads after a synchronisation. The observable rules
  * follow the reference's, including its quirks:
- *   - SplitVector() has no storage; reserve(n) on it allocates n elements and
- *     sets the size to n (splitvec.h:850-856); otherwise reserve grows to
- *     twice the request unless eco is set;
+ *   - SplitVector() has no storage; reserve(n) on it allocates exactly n
+ *     elements (splitvec.h:850-856); otherwise reserve grows to twice the
+ *     request unless eco is set;
  *   - device_push_back fills at most capacity - 1 elements (splitvec.h:1070-1078);
  *   - the iterator's postfix ++ and -- return the neighbour without moving
  *     the iterator (splitvec.h:1133-1136);
@@ -327,6 +327,7 @@ class SplitVector {
   void reserve(size_t n, bool eco = false, cudaStream_t = 0) {
     if (!data_) {
       allocate(n);
+      meta_[0] = 0;
       return;
     }
     if (n <= capacity()) return;

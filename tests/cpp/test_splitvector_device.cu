@@ -116,19 +116,22 @@ static void test_reference_device_tests() {
     cudaDeviceSynchronize();
     EXPECT_TRUE(a == b);
   }
-  {  // PushBack_And_Erase_Device: reserve on a default-constructed vector sizes it (size = capacity = 100),
-     // so every device_push_back fails; erase then drops the first element
+  {  // PushBack_And_Erase_Device: reserve on a default-constructed vector allocates exactly 100 (size 0);
+     // 32 device pushes fit; erase then drops the first element
     vec a;
     a.reserve(100);
-    EXPECT_TRUE(a.size() == 100 && a.capacity() == 100);
+    EXPECT_TRUE(a.size() == 0 && a.capacity() == 100);
     vec* da = a.upload();
     push_back_kernel<<<4, 8>>>(da);
     cudaDeviceSynchronize();
-    EXPECT_TRUE(a.size() == 100);
+    EXPECT_TRUE(a.size() == 32);
+    std::set<int> got(a.begin(), a.end()), want;
+    for (int i = 0; i < 32; ++i) want.insert(i);
+    EXPECT_TRUE(got == want);
     vec* db = a.upload();
     erase_kernel<<<1, 1>>>(db);
     cudaDeviceSynchronize();
-    EXPECT_TRUE(a.size() == 99);
+    EXPECT_TRUE(a.size() == 31);
   }
   {  // Test_CopyMetaData
     vec a(32, 42);
