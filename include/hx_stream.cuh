@@ -103,16 +103,25 @@ __device__ __forceinline__ unsigned warp_incl_scan(unsigned x, int lane) {
 }
 
 // ---- geometry and scratch -------------------------------------------------
+// Tuned on GB300 over slices of 8-32 KiB, 3-6 stages, deferral 1-3 and
+// 256/512-thread blocks (2^28 u32 copy_if and scan).
+#ifndef HX_STREAM_BLOCK
+#define HX_STREAM_BLOCK 256
+#endif
 #ifndef HX_STREAM_R
-#define HX_STREAM_R 4  // uint4 per thread per slice: 256 threads x 4 x 16 B = 16 KiB slices
+#define HX_STREAM_R 8  // uint4 per thread per slice: 256 threads x 8 x 16 B = 32 KiB slices
 #endif
 #ifndef HX_STREAM_STAGES
-#define HX_STREAM_STAGES 6
+#define HX_STREAM_STAGES 3
 #endif
 #ifndef HX_STREAM_DEFER
-#define HX_STREAM_DEFER 2
+#define HX_STREAM_DEFER 1
 #endif
-constexpr int kBlock = 256;
+#ifndef HX_STREAM_MINB
+#define HX_STREAM_MINB 1  // CTAs per SM the register allocation must allow
+#endif
+constexpr int kBlock = HX_STREAM_BLOCK;
+static_assert(kBlock % 32 == 0 && kBlock <= 1024, "whole warps, at most 32 of them");
 constexpr int kR = HX_STREAM_R;
 constexpr int kStages = HX_STREAM_STAGES;
 constexpr int kDefer = HX_STREAM_DEFER;
@@ -198,7 +207,7 @@ struct Done {                              // what the pass reports, and where i
 // order, writes beyond `capacity` dropped, c to *done.d_count.
 // ---------------------------------------------------------------------------
 template <class T, class O, class Sel, bool SCAN>
-__global__ void __launch_bounds__(kBlock) k_stream(const T* __restrict__ in, O* __restrict__ out, uint64_t n,
+__global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __restrict__ in, O* __restrict__ out, uint64_t n,
                                                   Sel sel, uint64_t capacity, Done done, Scratch sc) {
   constexpr int E = 16 / sizeof(T);
   constexpr int WARPS = kBlock / 32;
