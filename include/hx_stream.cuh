@@ -7,8 +7,8 @@
 // unit; libhx instantiates it for its predicate descriptors.
 //
 // Shape. One cooperative launch of G co-resident CTAs (G = resident CTAs per
-// SM x SMs). The input is cut into slices of SLICE elements (one stage of
-// shared memory, 16 KiB by default); phase p gives slice p*G + b to CTA b, so
+// SM x SMs). The input is cut into slices (one stage of shared memory, 64 KiB
+// by default); phase p gives slice p*G + b to CTA b, so
 // a phase is G consecutive slices. Each CTA keeps STAGES slices in flight,
 // each filled by one bulk copy (cp.async.bulk, completion on an mbarrier).
 //   pass 1, phase p: read the slice from shared memory, evaluate the rule (or
@@ -103,13 +103,13 @@ __device__ __forceinline__ unsigned warp_incl_scan(unsigned x, int lane) {
 }
 
 // ---- geometry and scratch -------------------------------------------------
-// Tuned on GB300 over slices of 8-32 KiB, 3-6 stages, deferral 1-3 and
-// 256/512-thread blocks (2^28 u32 copy_if and scan).
+// Tuned on GB300 over slices of 8-64 KiB, 3-6 stages, deferral 1-3 and
+// 256/512/768/1024-thread blocks (2^28 u32 copy_if and scan).
 #ifndef HX_STREAM_BLOCK
-#define HX_STREAM_BLOCK 256
+#define HX_STREAM_BLOCK 512
 #endif
 #ifndef HX_STREAM_R
-#define HX_STREAM_R 8  // uint4 per thread per slice: 256 threads x 8 x 16 B = 32 KiB slices
+#define HX_STREAM_R 8  // uint4 per thread per slice: 512 threads x 8 x 16 B = 64 KiB slices
 #endif
 #ifndef HX_STREAM_STAGES
 #define HX_STREAM_STAGES 3
@@ -129,7 +129,7 @@ static_assert(kDefer >= 1 && kDefer < kStages, "a stage must be free to load whi
 // Count slots per CTA: a CTA overwrites the slot of phase p - kSlots only
 // after every CTA has read it (see the kernel), which needs 2 * D + 2 slots.
 constexpr int kSlots = 2 * kDefer + 2;
-constexpr int kMaxGrid = 2048;
+constexpr int kMaxGrid = 1024;  // CTAs at most (GB300: 152 SMs x 1-2 CTAs); a larger device runs 1024
 constexpr int kSlotLoads = kMaxGrid / kBlock;  // count slots each thread reads per phase
 constexpr unsigned kSliceBytes = kBlock * kR * 16;
 

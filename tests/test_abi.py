@@ -84,9 +84,9 @@ def test_null_handles_and_outputs_are_rejected(hx):
 def test_scratch_sizes_and_undersized_caller_scratch(hx):
     """hx_scratch_bytes: the scan needs the larger of its two kernels' scratch — a 256-byte header and one
     8-byte status per 12288-element tile (buffers that are not 16-byte aligned), or a 256-byte header and
-    2 * 2 + 2 count slots of 8 bytes for each CTA, at most one CTA per 4096-element slice and 2048 CTAs (the
-    phase-partitioned kernel); copy_if needs at least as much plus a 256-byte count area, never shrinking as
-    n grows. A caller buffer smaller than
+    2 * 1 + 2 count slots of 8 bytes for each CTA, at most one CTA per 16384-element (64 KiB) slice and 1024
+    CTAs (the phase-partitioned kernel); copy_if needs at least as much plus a 256-byte count area, never
+    shrinking as n grows. A caller buffer smaller than
     the need is rejected before any device work: every call here is one that must be rejected, so the fake
     pointers are never dereferenced."""
     lib = hx.lib()
@@ -98,7 +98,7 @@ def test_scratch_sizes_and_undersized_caller_scratch(hx):
 
     for n in (0, 1, 4095, 4096, 4097, 1 << 20, (1 << 28) + 3):
         assert need(hx.SCRATCH_SCAN, n) == max(256 + 8 * max(1, -(-n // 12288)),
-                                               256 + 8 * 6 * min(2048, max(1, -(-n // 4096))))
+                                               256 + 8 * 4 * min(1024, max(1, -(-n // 16384))))
     prev = 0
     for n in (0, 1, 100, 5000, 1 << 16, 1 << 20, 1 << 24):
         c = need(hx.SCRATCH_COPY_IF, n)
