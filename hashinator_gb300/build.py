@@ -46,7 +46,8 @@ def _stale(target: Path, deps) -> bool:
 def build_lib(verbose: bool = False, force: bool = False) -> Path:
     nvcc = _nvcc()
     BUILD.mkdir(exist_ok=True)
-    headers = sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [ROOT / "include" / "hx.h"]
+    headers = (sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted((ROOT / "include").glob("*.h"))
+               + sorted((ROOT / "include").glob("*.cuh")))
     srcs = [CSRC / s for s in CUDA_SOURCES if (CSRC / s).exists()]
     objs = []
     procs = []
