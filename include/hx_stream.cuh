@@ -130,7 +130,7 @@ static_assert(kDefer >= 1 && kDefer < kStages, "a stage must be free to load whi
 // after every CTA has read it (see the kernel), which needs 2 * D + 2 slots.
 constexpr int kSlots = 2 * kDefer + 2;
 constexpr int kMaxGrid = 1024;  // CTAs at most (GB300: 152 SMs x 1-2 CTAs); a larger device runs 1024
-constexpr int kSlotLoads = kMaxGrid / kBlock;  // count slots each thread reads per phase
+constexpr int kSlotLoads = (kMaxGrid + kBlock - 1) / kBlock;  // count slots each thread reads per phase
 constexpr unsigned kSliceBytes = kBlock * kR * 16;
 
 // Scratch: [error word u32][pad .. 256 B][count slots u64 x kSlots x grid].
