@@ -1030,7 +1030,7 @@ def run_ours(args):
     achieved = ins_gbs if dominant == "insert" else q_gbs
     # measured traffic (2^26 keys) exists for the thread-per-key insert and query kernels
     tag = ("insert_u32_lf050" if args.group in (0, 1) else None) if dominant == "insert" else \
-        ("query_t1_u32_lf050" if args.group == 1 else None)
+        ("query_t1_u32_lf050" if args.group == 1 else ("query_u32_lf050" if args.group == 0 else None))
     traffic = traffic_from_profiles(tag) if tag and args.log_keys == 26 else None
     dom_keys_s = n / (t_ins if dominant == "insert" else t_q)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
