@@ -1129,16 +1129,12 @@ def run_case(args):
     o = torch.empty_like(dq)
     stream = torch.cuda.Stream(device=dev)
     m = hx.Hashmap(sp, w, stream=stream)
-    m.set_insert_partition(args.case_partition)
-    t_clear = _ev_time(stream, lambda: m.clear(stream=stream), reps=args.case_reps)
     t_ins = _ev_time(stream, lambda: (m.clear(stream=stream), m.insert(dk, dv, target_lf=0.0, stream=stream)),
                      reps=args.case_reps)
     t_q = _ev_time(stream, lambda: m.retrieve(dq, o, stream=stream), reps=args.case_reps)
     inf = m.info(stream=stream)
     print(json.dumps({"case": f"u{8 * w} 2^{sp} buckets LF {args.case_lf}", "keys": n, "fill": int(inf.fill),
-                      "partition": args.case_partition, "clear_ms": round(t_clear * 1e3, 3),
-                      "clear_plus_insert_ms": round(t_ins * 1e3, 3), "query_ms": round(t_q * 1e3, 3),
-                      "insert_Mkeys_s": round(n / (t_ins - t_clear) / 1e6, 1)}), flush=True)
+                      "clear_plus_insert_ms": round(t_ins * 1e3, 3), "query_ms": round(t_q * 1e3, 3)}), flush=True)
     m.close()
     return 0
 
@@ -1173,8 +1169,6 @@ def main():
     ap.add_argument("--case-kind", default="map", choices=["map", "copy_if", "scan"])
     ap.add_argument("--case-log-n", type=int, default=26)
     ap.add_argument("--case-s", type=int, default=1, help="copy_if selectivity in percent")
-    ap.add_argument("--case-partition", type=int, default=-1, choices=[-1, 0, 1],
-                    help="insert reordering by table region: -1 automatic, 0 never, 1 always")
     args = ap.parse_args()
     if args.case:
         return run_case(args)

@@ -126,7 +126,6 @@ _SIGS = {
     "hx_bucket_data": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64)],
     "hx_map_set_tuning": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int],
     "hx_map_set_insert_mode": [ctypes.c_void_p, ctypes.c_int],
-    "hx_map_set_insert_partition": [ctypes.c_void_p, ctypes.c_int],
     "hx_map_set_window_bytes": [ctypes.c_void_p, ctypes.c_int],
     "hx_set_l2_fetch_granularity": [ctypes.c_int],
     "hx_diag_random_access": [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p],
@@ -403,10 +402,6 @@ class Hashmap:
 
     def set_insert_mode(self, blind_cas: bool) -> None:
         _check(self._h.hx_map_set_insert_mode(self._m, 1 if blind_cas else 0), "hx_map_set_insert_mode")
-
-    def set_insert_partition(self, mode: int) -> None:
-        """-1 automatic (the default), 0 never, 1 always reorder an insert batch by table region first."""
-        _check(self._h.hx_map_set_insert_partition(self._m, mode), "hx_map_set_insert_partition")
 
     # metadata (synchronous) ----------------------------------------------
     def info(self, stream=None) -> Info:

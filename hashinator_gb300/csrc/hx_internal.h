@@ -15,7 +15,6 @@ struct Tuning {
   int block = 256;
   bool blind = true;  // thread-per-key insert: CAS the home bucket without reading it first
   bool wide = false;  // thread-per-key windows of 64 B instead of 32 B
-  int partition = -1; // insert batch reordered by table region first: -1 automatic, 0 never, 1 always
 };
 
 
@@ -32,10 +31,6 @@ struct hx_map {
   uint64_t scratch_bytes = 0;
   hx::Tuning tune;
   std::mutex mu;  // guards scratch growth; a map is not thread-safe otherwise
-  void* part = nullptr;  // the region-ordered copy of an insert batch (hx_partition.cuh)
-  uint64_t part_bytes = 0;
-  cudaEvent_t part_done = nullptr;  // recorded after the last insert that read `part`
-  bool owned = false;  // created by hx_map_create (not a view into a batch or a server)
 };
 
 

@@ -14,7 +14,6 @@
 #include "hx_internal.h"
 #include "hx_probe.cuh"
 #include "hx_scan.cuh"
-#include "hx_partition.cuh"
 
 namespace hx {
 
@@ -530,111 +529,11 @@ static unsigned grid_for(F kernel, uint64_t work_threads, int block) {
     }                                                            \
   } while (0)
 
-// Region bits for a table of 2^sp buckets of pbytes each: regions of about
-// 1 MiB (at most kPartMaxRegions of them).
-static int part_rbits(int sp, int pbytes) {
-  int lg = 0;
-  while ((1 << lg) < pbytes) ++lg;
-  int r = sp + lg - 20;
-  if (r < 0) r = 0;
-  if ((1 << r) > kPartMaxRegions) {
-    r = 0;
-    while ((2 << r) <= kPartMaxRegions) ++r;
-  }
-  return r;
-}
-
-// Whether an insert of n keys is reordered by table region first: for tables
-// far larger than L2 and large batches (automatic), or as the tuning says.
-// Only maps created by hx_map_create own the reordering buffer.
-template <class P>
-static bool want_partition(const hx_map* m, uint64_t n) {
-  if (!m->owned || m->tune.partition == 0 || n < 2) return false;
-  if (part_rbits(m->sp, (int)sizeof(P)) < 4) return false;
-  if (m->tune.partition == 1) return true;
-  return n >= (1ull << 20) && (nslots(m) * sizeof(P)) >= (256ull << 20);
-}
-
-// The region-ordered copy of an insert batch in m->part: counts, cursors,
-// then the keys and values (or the pairs). Redirects *keys / *vals / *pairs
-// to it.
-template <class P>
-static hx_status partition_batch(hx_map* m, const void** keys, const void** vals, const void** pairs, uint64_t n,
-                                 cudaStream_t s) {
-  using K = typename PairTraits<P>::K;
-  using V = typename PairTraits<P>::V;
-  const int rbits = part_rbits(m->sp, (int)sizeof(P));
-  const uint64_t hdr = 256 * ((kPartMaxRegions * (4 + 8) + 255) / 256);
-  const uint64_t body = *pairs ? n * sizeof(P) : n * (sizeof(K) + sizeof(V));
-  const uint64_t need = hdr + body + 256;
-  // an insert on another stream may still be reading the buffer: order after it
-  if (m->part_done) HX_CUDA(cudaStreamWaitEvent(s, m->part_done, 0));
-  else HX_CUDA(cudaEventCreateWithFlags(&m->part_done, cudaEventDisableTiming));
-  if (m->part_bytes < need) {
-    if (m->part) HX_CUDA(cudaFreeAsync(m->part, s));
-    m->part = nullptr;
-    m->part_bytes = 0;
-    HX_CUDA(cudaMallocAsync(&m->part, need, s));
-    m->part_bytes = need;
-  }
-  char* base = static_cast<char*>(m->part);
-  unsigned* counts = reinterpret_cast<unsigned*>(base);
-  unsigned long long* cursor = reinterpret_cast<unsigned long long*>(base + kPartMaxRegions * 4);
-  char* data = base + hdr;
-  K* ok = reinterpret_cast<K*>(data);
-  V* ov = reinterpret_cast<V*>(data + ((n * sizeof(K) + 255) / 256) * 256);
-  P* op = reinterpret_cast<P*>(data);
-  HX_CUDA(cudaMemsetAsync(counts, 0, (size_t)4 << rbits, s));
-  const int sms = sm_count();
-  const unsigned hist_grid = (unsigned)std::min<uint64_t>((n + kPartBlock - 1) / kPartBlock, (uint64_t)sms * 4);
-  const unsigned scat_grid = (unsigned)std::min<uint64_t>((n + kPartChunk - 1) / kPartChunk, (uint64_t)sms * 2);
-  constexpr size_t smem = part_scatter_smem<P>();
-  if (*pairs) {
-    k_region_hist<P, true><<<hist_grid, kPartBlock, 0, s>>>(nullptr, static_cast<const P*>(*pairs), n, m->sp, rbits,
-                                                            counts);
-    HX_CUDA(cudaGetLastError());
-    k_region_scan<<<1, kPartBlock, 0, s>>>(counts, cursor, rbits);
-    HX_CUDA(cudaGetLastError());
-    auto kern = k_region_scatter<P, true>;
-    HX_CUDA(allow_dynamic_smem(kern, smem));
-    kern<<<scat_grid, kPartBlock, smem, s>>>(nullptr, nullptr, static_cast<const P*>(*pairs), n, m->sp, rbits, cursor,
-                                             nullptr, nullptr, op);
-    HX_CUDA(cudaGetLastError());
-    *pairs = op;
-  } else {
-    k_region_hist<P, false><<<hist_grid, kPartBlock, 0, s>>>(static_cast<const K*>(*keys), nullptr, n, m->sp,
-                                                             rbits, counts);
-    HX_CUDA(cudaGetLastError());
-    k_region_scan<<<1, kPartBlock, 0, s>>>(counts, cursor, rbits);
-    HX_CUDA(cudaGetLastError());
-    auto kern = k_region_scatter<P, false>;
-    HX_CUDA(allow_dynamic_smem(kern, smem));
-    kern<<<scat_grid, kPartBlock, smem, s>>>(static_cast<const K*>(*keys), static_cast<const V*>(*vals), nullptr, n,
-                                             m->sp, rbits, cursor, ok, ov, nullptr);
-    HX_CUDA(cudaGetLastError());
-    *keys = ok;
-    *vals = ov;
-  }
-  for (int i = 0; i < 3; ++i) {  // the three launches, for hx_kernel_launch_count
-    const hx_status st = after_launch();
-    if (st != HX_OK) return st;
-  }
-  return HX_OK;
-}
-
 template <class P>
 static hx_status launch_insert(hx_map* m, const void* keys, const void* vals, const void* pairs, uint64_t n,
-                               const unsigned long long* d_n, cudaStream_t s, bool reordered = false) {
+                               const unsigned long long* d_n, cudaStream_t s) {
   using K = typename PairTraits<P>::K;
   using V = typename PairTraits<P>::V;
-  if (!reordered && !d_n && want_partition<P>(m, n)) {
-    hx_status st = partition_batch<P>(m, &keys, &vals, &pairs, n, s);
-    if (st != HX_OK) return st;
-    st = launch_insert<P>(m, keys, vals, pairs, n, d_n, s, true);
-    if (st != HX_OK) return st;
-    HX_CUDA(cudaEventRecord(m->part_done, s));
-    return HX_OK;
-  }
   // clean_tombstones re-inserts its moved keys (count on the device) into a
   // table whose fill bound still counts the erased keys: thread-per-key
   const Policy pol = (d_n && m->tune.group == 0) ? Policy{1, 1} : policy(m, Op::INSERT);
@@ -909,7 +808,6 @@ hx_status hx_map_create(hx_map** out, int key_bytes, int val_bytes, int size_pow
   if (size_power < 1 || size_power > 31) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   hx_map* m = new hx_map();
-  m->owned = true;
   m->key_bytes = key_bytes;
   m->val_bytes = val_bytes;
   m->sp = size_power;
@@ -944,8 +842,6 @@ hx_status hx_map_destroy(hx_map* m) {
   if (m->buckets) cudaFree(m->buckets);
   if (m->info) cudaFree(m->info);
   if (m->scratch) cudaFree(m->scratch);
-  if (m->part) cudaFree(m->part);
-  if (m->part_done) cudaEventDestroy(m->part_done);
   delete m;
   return e == cudaSuccess ? HX_OK : cuda_status(e);
 }
@@ -1177,12 +1073,6 @@ hx_status hx_bucket_data(hx_map* m, void** d_buckets, uint64_t* bucket_count) {
 hx_status hx_map_set_insert_mode(hx_map* m, int blind_cas) {
   if (!m) return HX_ERR_INVALID_ARG;
   m->tune.blind = blind_cas != 0;
-  return HX_OK;
-}
-
-hx_status hx_map_set_insert_partition(hx_map* m, int mode) {
-  if (!m || mode < -1 || mode > 1) return HX_ERR_INVALID_ARG;
-  m->tune.partition = mode;
   return HX_OK;
 }
 

@@ -239,16 +239,6 @@ hx_status hx_map_set_tuning(hx_map* map, int group_width, int keys_per_thread, i
  * 0 loads each key's first window and CASes into it afterwards. */
 hx_status hx_map_set_insert_mode(hx_map* map, int blind_cas);
 
-/* Insert reordering (no reference counterpart): with mode 1 every insert
- * first copies its batch into a map-owned buffer in the order of the table
- * region (about 1 MiB of buckets) each key's home bucket lies in, and inserts
- * that copy, so that the bucket updates of the running kernel stay within a
- * few regions; with 0 it never does; -1 (the default) does it for batches of
- * 2^20 keys and more into tables of 256 MiB and more. The mapping is the same
- * either way. The buffer (key and value bytes per key of the largest batch)
- * is kept until the map is destroyed. */
-hx_status hx_map_set_insert_partition(hx_map* map, int mode);
-
 /* Thread-per-key window: 32 (one DRAM sector) or 64 bytes of buckets per
  * probe step. No reference counterpart. */
 hx_status hx_map_set_window_bytes(hx_map* map, int bytes);
