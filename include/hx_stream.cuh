@@ -316,13 +316,22 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
         } else {
           const uint64_t e = e0 + (uint64_t)(wbase + r * 32 + lane) * E;
           unsigned m = 0;
+          if (whole) {  // block-uniform: no per-element bounds checks in a whole slice
 #pragma unroll
-          for (int q = 0; q < E; ++q) {
-            const bool in_range = whole || e + q < n;
-            const bool s = in_range && sel(x[r][q]);
-            if (s) m |= 1u << q;
-            if constexpr (Sel::kRewrites) {
-              if (in_range) sel.rewrite(const_cast<T*>(in), e + q, x[r][q], s);
+            for (int q = 0; q < E; ++q) {
+              const bool s = sel(x[r][q]);
+              m |= (unsigned)s << q;
+              if constexpr (Sel::kRewrites) sel.rewrite(const_cast<T*>(in), e + q, x[r][q], s);
+            }
+          } else {
+#pragma unroll
+            for (int q = 0; q < E; ++q) {
+              const bool in_range = e + q < n;
+              const bool s = in_range && sel(x[r][q]);
+              if (s) m |= 1u << q;
+              if constexpr (Sel::kRewrites) {
+                if (in_range) sel.rewrite(const_cast<T*>(in), e + q, x[r][q], s);
+              }
             }
           }
           bits[r] = m;
@@ -357,6 +366,7 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
         O* packed = reinterpret_cast<O*>(stage);
 #pragma unroll
         for (int r = 0; r < kR; ++r) {
+          if (!bits[r]) continue;  // nothing selected in this uint4: the common case for a sparse rule
           unsigned o = woff + pre[r];
 #pragma unroll
           for (int q = 0; q < E; ++q)
