@@ -307,6 +307,7 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
       unsigned pre[kR];
       unsigned acc = 0;
       unsigned bits[kR];
+      unsigned cnt[kR];
 #pragma unroll
       for (int r = 0; r < kR; ++r) {
         unsigned c;
@@ -337,9 +338,34 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
           bits[r] = m;
           c = __popc(m);
         }
-        const unsigned incl = warp_incl_scan(c, lane);
-        pre[r] = acc + incl - c;
-        acc += __shfl_sync(0xffffffffu, incl, 31);
+        cnt[r] = c;
+        if constexpr (SCAN) {
+          const unsigned incl = warp_incl_scan(c, lane);
+          pre[r] = acc + incl - c;
+          acc += __shfl_sync(0xffffffffu, incl, 31);
+        }
+      }
+      if constexpr (!SCAN) {
+        // Ranks of the selections: a lane's count per uint4 is at most 4 and a
+        // warp's sum at most 128, so four uint4s share one 32-bit word as byte
+        // lanes with no carries between them: one warp scan per four uint4s.
+        constexpr int NW = (kR + 3) / 4;
+        unsigned packed_c[NW], incl_w[NW], tot_w[NW];
+#pragma unroll
+        for (int w = 0; w < NW; ++w) packed_c[w] = 0;
+#pragma unroll
+        for (int r = 0; r < kR; ++r) packed_c[r / 4] |= cnt[r] << (8 * (r % 4));
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+          incl_w[w] = warp_incl_scan(packed_c[w], lane);
+          tot_w[w] = __shfl_sync(0xffffffffu, incl_w[w], 31);
+        }
+#pragma unroll
+        for (int r = 0; r < kR; ++r) {
+          const unsigned incl = (incl_w[r / 4] >> (8 * (r % 4))) & 0xffu;
+          pre[r] = acc + incl - cnt[r];
+          acc += (tot_w[r / 4] >> (8 * (r % 4))) & 0xffu;
+        }
       }
       if (lane == 0) s_warp[warp] = acc;
       __syncthreads();
