@@ -707,6 +707,7 @@ def run_streaming(args, stream, dev, peak):
                                  "frac": round((4 * n + 4 * c) / t / 1e9 / peak, 4),
                                  "exact": bool(int(dc.item()) == len(want) and np.array_equal(got, want))}
         del want, got
+    res["copy_if_functor"] = _guarded(lambda: functor_leg(args.stream_log_n))
     y = (x & 15).contiguous()
     y_h = (x_h & np.uint32(15))
     del r_h
@@ -756,6 +757,80 @@ def run_streaming(args, stream, dev, peak):
     del b, valid, sel, want
     m.close()
     return res
+
+
+FUNCTOR_LEG_SRC = r"""
+// copy_if with a caller's functor through the drop-in header (the rule compiled
+// into the single-pass kernel in this translation unit) against libhx's
+// descriptor copy_if, on the same 2^k uniform u32 elements.
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+#include "hashinator_compat.h"
+struct ModLt {
+  uint32_t a, b;
+  __host__ __device__ bool operator()(const uint32_t& x) const { return x % a < b; }
+};
+__global__ void k_gen(uint32_t* x, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    unsigned long long z = (i + 0x9E3779B97F4A7C15ull) * 0xBF58476D1CE4E5B9ull;
+    z ^= z >> 31; z *= 0x94D049BB133111EBull; z ^= z >> 29;
+    x[i] = (uint32_t)z;
+  }
+}
+int main(int argc, char** argv) {
+  const size_t n = (size_t)1 << atoi(argv[1]);
+  uint32_t *x, *o1, *o2; size_t* c1; void* sc;
+  cudaMalloc(&x, n * 4); cudaMalloc(&o1, n * 4); cudaMalloc(&o2, n * 4); cudaMalloc(&c1, 8);
+  const size_t need = split::tools::detail::compaction_scratch_bytes<uint32_t>(n);
+  cudaMalloc(&sc, need);
+  k_gen<<<4096, 256>>>(x, n);
+  cudaStream_t s; cudaStreamCreate(&s);
+  cudaEvent_t e0, e1; cudaEventCreate(&e0); cudaEventCreate(&e1);
+  std::printf("{");
+  for (uint32_t sel : {1u, 50u, 99u}) {
+    float best = 1e9f;
+    for (int rep = 0; rep < 6; ++rep) {
+      cudaEventRecord(e0, s);
+      split::tools::detail::compact(x, o1, n, n, ModLt{100, sel}, split::tools::detail::Identity{}, c1, ~(size_t)0, sc, s);
+      cudaEventRecord(e1, s); cudaEventSynchronize(e1);
+      float ms; cudaEventElapsedTime(&ms, e0, e1);
+      if (rep && ms < best) best = ms;
+    }
+    size_t fc = 0; uint64_t dc = 0;
+    cudaMemcpy(&fc, c1, 8, cudaMemcpyDeviceToHost);
+    hx_pred p{HX_PRED_MOD_LT, HX_FIELD_ELEM, 0, 0, 100, sel};
+    hx_copy_if(x, o2, n, 4, &p, n, nullptr, &dc, nullptr, 0, s);
+    std::vector<uint32_t> a(fc), b(dc);
+    cudaMemcpy(a.data(), o1, fc * 4, cudaMemcpyDeviceToHost);
+    cudaMemcpy(b.data(), o2, dc * 4, cudaMemcpyDeviceToHost);
+    std::printf("%s\"s%u\": {\"ms\": %.4f, \"selected\": %zu, \"equal_to_descriptor\": %s}", sel == 1 ? "" : ", ", sel,
+                best, fc, (fc == dc && a == b) ? "true" : "false");
+  }
+  std::printf("}\n");
+  return cudaDeviceSynchronize() != cudaSuccess;
+}
+"""
+
+
+def functor_leg(log_n: int) -> dict:
+    """The drop-in header's functor copy_if (a caller's rule compiled into the single-pass kernel) timed with CUDA
+    events on 2^log_n uniform u32, and compared element for element with libhx's descriptor copy_if. The program is
+    built with nvcc into hashinator_gb300/_build/ once."""
+    from hashinator_gb300 import build
+    bdir = ROOT / "hashinator_gb300" / "_build"
+    bdir.mkdir(exist_ok=True)
+    src, exe = bdir / "functor_copy_if.cu", bdir / "functor_copy_if"
+    if not exe.exists() or not src.exists() or src.read_text() != FUNCTOR_LEG_SRC:
+        src.write_text(FUNCTOR_LEG_SRC)
+        lib_dir = str(ROOT / "hashinator_gb300")
+        subprocess.run([build._nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+                        "-I", str(ROOT / "include"), str(src), "-o", str(exe), "-L", lib_dir, "-lhx",
+                        f"-Xlinker=-rpath,{lib_dir}"], check=True, capture_output=True, timeout=600)
+    r = subprocess.run([str(exe), str(log_n)], capture_output=True, text=True, timeout=600, check=True)
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    out["rule"] = "struct ModLt { x % 100 < s } through split::tools (hashinator_compat.h), CUDA events"
+    return out
 
 
 def run_reference(args):
@@ -811,6 +886,10 @@ def _summary(line: dict) -> dict:
     if isinstance(st, dict):
         out["streaming_ms"] = {k: v.get("ms") for k, v in st.items() if isinstance(v, dict)}
         out["streaming_exact"] = all(v.get("exact", True) for v in st.values() if isinstance(v, dict))
+        fl = st.get("copy_if_functor")
+        if isinstance(fl, dict) and "s1" in fl:
+            out["copy_if_functor_ms"] = {k: v["ms"] for k, v in fl.items() if isinstance(v, dict)}
+            out["copy_if_functor_equal"] = all(v["equal_to_descriptor"] for v in fl.values() if isinstance(v, dict))
     sw = g(line, "large_map_lf_sweep", "runs")
     if isinstance(sw, list):
         out["lf_sweep_exact"] = all(r.get("query_exact") and r.get("requery_exact") for r in sw)
