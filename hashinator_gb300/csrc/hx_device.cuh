@@ -180,4 +180,19 @@ __device__ __forceinline__ bool pred_pair(const hx_pred& pr, typename PairTraits
   return r;
 }
 
+// pred_pair for a bucket at index i of a table of 2^sp buckets: HX_PRED_NOT_HOME
+// becomes "i is not the key's home bucket" — the same answer as reading the
+// home bucket and finding another key there (every key occurs once), with no
+// read of the table.
+template <class P>
+__device__ __forceinline__ bool pred_pair_at(const hx_pred& pr, typename PairTraits<P>::K k,
+                                             typename PairTraits<P>::V v, uint64_t i, int sp) {
+  if (pr.op != HX_PRED_NOT_HOME) return pred_pair<P>(pr, k, v, TableRef<P>{nullptr, sp});
+  using Tr = PairTraits<P>;
+  const bool sentinel = (k == Tr::EMPTY) || (k == Tr::TOMB);
+  bool r = !sentinel && (uint64_t)home_slot(k, sp) != i;
+  if (pr.flags & HX_PRED_NEGATE) r = !r;
+  return r;
+}
+
 }  // namespace hx

@@ -564,6 +564,13 @@ struct PredSel {
   typename ElemOps<T>::Ctx ctx;
   uint64_t thresh = 0;  // PK_MOD_LT_THRESH: s * magic
   static constexpr bool kRewrites = CLEAN;
+  // generic pair rules may be HX_PRED_NOT_HOME, which compares a bucket's
+  // index with its key's home bucket
+  static constexpr bool kIndexed = PK == PK_GENERIC && !std::is_same<T, uint32_t>::value;
+  __device__ __forceinline__ bool at(const T& x, uint64_t i) const {
+    if constexpr (kIndexed) return pred_pair_at<T>(pr, x.first, x.second, i, ctx.sp);
+    else return (*this)(x);
+  }
   __device__ __forceinline__ bool operator()(const T& x) const {
     if constexpr (PK == PK_MOD_LT_THRESH) {
       uint32_t f;

@@ -535,6 +535,7 @@ template <typename Rule>
 struct RuleSel {
   Rule rule;
   static constexpr bool kRewrites = false;
+  static constexpr bool kIndexed = false;
   template <class T>
   __device__ __forceinline__ bool operator()(const T& x) const {
     Rule r = rule;

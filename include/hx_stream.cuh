@@ -168,11 +168,14 @@ __device__ __forceinline__ O project(const T& x) {
 //   __device__ bool operator()(const T& x) const;
 //   static constexpr bool kRewrites;   // true: called as below for every element of the input
 //   __device__ void rewrite(T* in, uint64_t i, const T& x, bool selected) const;
-// kRewrites lets the clean_tombstones pass empty the buckets it takes out.
+//   static constexpr bool kIndexed;    // true: the rule is called as at(x, i), i the element's index
+// kRewrites lets the clean_tombstones pass empty the buckets it takes out;
+// kIndexed lets a rule depend on where the element sits (a bucket's home).
 template <class F>
 struct FunctorSel {
   F f;
   static constexpr bool kRewrites = false;
+  static constexpr bool kIndexed = false;
   template <class T>
   __device__ __forceinline__ bool operator()(const T& x) const {
     return f(x);
@@ -182,6 +185,7 @@ struct FunctorSel {
 };
 struct ScanSel {  // placeholder selector of the scan
   static constexpr bool kRewrites = false;
+  static constexpr bool kIndexed = false;
   template <class T>
   __device__ __forceinline__ bool operator()(const T&) const {
     return true;
@@ -320,7 +324,9 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
           if (whole) {  // block-uniform: no per-element bounds checks in a whole slice
 #pragma unroll
             for (int q = 0; q < E; ++q) {
-              const bool s = sel(x[r][q]);
+              bool s;
+              if constexpr (Sel::kIndexed) s = sel.at(x[r][q], e + q);
+              else s = sel(x[r][q]);
               m |= (unsigned)s << q;
               if constexpr (Sel::kRewrites) sel.rewrite(const_cast<T*>(in), e + q, x[r][q], s);
             }
@@ -328,7 +334,11 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
 #pragma unroll
             for (int q = 0; q < E; ++q) {
               const bool in_range = e + q < n;
-              const bool s = in_range && sel(x[r][q]);
+              bool s = false;
+              if (in_range) {
+                if constexpr (Sel::kIndexed) s = sel.at(x[r][q], e + q);
+                else s = sel(x[r][q]);
+              }
               if (s) m |= 1u << q;
               if constexpr (Sel::kRewrites) {
                 if (in_range) sel.rewrite(const_cast<T*>(in), e + q, x[r][q], s);
