@@ -767,9 +767,9 @@ FUNCTOR_LEG_SRC = r"""
 #include <cstdlib>
 #include <vector>
 #include "hashinator_compat.h"
-struct ModLt {
-  uint32_t a, b;
-  __host__ __device__ bool operator()(const uint32_t& x) const { return x % a < b; }
+struct ModLt {  // x % 100 < b, the divisor a constant as in the reference's own test rules
+  uint32_t b;
+  __host__ __device__ bool operator()(const uint32_t& x) const { return x % 100u < b; }
 };
 __global__ void k_gen(uint32_t* x, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
@@ -792,7 +792,7 @@ int main(int argc, char** argv) {
     float best = 1e9f;
     for (int rep = 0; rep < 6; ++rep) {
       cudaEventRecord(e0, s);
-      split::tools::detail::compact(x, o1, n, n, ModLt{100, sel}, split::tools::detail::Identity{}, c1, ~(size_t)0, sc, s);
+      split::tools::detail::compact(x, o1, n, n, ModLt{sel}, split::tools::detail::Identity{}, c1, ~(size_t)0, sc, s);
       cudaEventRecord(e1, s); cudaEventSynchronize(e1);
       float ms; cudaEventElapsedTime(&ms, e0, e1);
       if (rep && ms < best) best = ms;
@@ -829,7 +829,7 @@ def functor_leg(log_n: int) -> dict:
                         f"-Xlinker=-rpath,{lib_dir}"], check=True, capture_output=True, timeout=600)
     r = subprocess.run([str(exe), str(log_n)], capture_output=True, text=True, timeout=600, check=True)
     out = json.loads(r.stdout.strip().splitlines()[-1])
-    out["rule"] = "struct ModLt { x % 100 < s } through split::tools (hashinator_compat.h), CUDA events"
+    out["rule"] = "struct ModLt { x % 100u < s } (constant divisor) through split::tools (hashinator_compat.h), CUDA events"
     return out
 
 
@@ -884,7 +884,7 @@ def _summary(line: dict) -> dict:
            "checks_exact": all(v for k, v in (line.get("checks") or {}).items() if isinstance(v, bool))}
     st = line.get("streaming")
     if isinstance(st, dict):
-        out["streaming_ms"] = {k: v.get("ms") for k, v in st.items() if isinstance(v, dict)}
+        out["streaming_ms"] = {k: v.get("ms") for k, v in st.items() if isinstance(v, dict) and "ms" in v}
         out["streaming_exact"] = all(v.get("exact", True) for v in st.values() if isinstance(v, dict))
         fl = st.get("copy_if_functor")
         if isinstance(fl, dict) and "s1" in fl:

@@ -638,6 +638,10 @@ hx_status hx_batch_plan_create(hx_batch* b, const hx_batch_work* w, hx_batch_pla
   HX_RANGE("hx_batch_plan_create");
   if (!b || !w || !out) return HX_ERR_INVALID_ARG;
   *out = nullptr;
+  const unsigned kb = (unsigned)b->key_bytes;
+  if (misaligned(w->ins_keys, kb) || misaligned(w->ins_vals, kb) || misaligned(w->query_keys, kb) ||
+      misaligned(w->query_out, kb) || misaligned(w->erase_keys, kb))
+    return HX_ERR_INVALID_ARG;
   const unsigned nm = b->n_maps;
   hx_batch_plan* p = new hx_batch_plan();
   p->b = b;

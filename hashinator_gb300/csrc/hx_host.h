@@ -42,6 +42,13 @@ hx_status after_launch();
 
 int sm_count();  // SMs of the current device (cached per device)
 
+// A device array of elements of `align` bytes must start at a multiple of
+// `align`: the kernels load and store whole elements (and pairs as one 8- or
+// 16-byte access), so a misaligned pointer is rejected before any launch.
+inline bool misaligned(const void* p, unsigned align) {
+  return (reinterpret_cast<uintptr_t>(p) % align) != 0;
+}
+
 // Blocks per SM for a kernel at a block size (cached by the caller).
 template <class F>
 int blocks_per_sm(F kernel, int block, size_t smem = 0) {

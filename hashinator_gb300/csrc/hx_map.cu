@@ -419,6 +419,7 @@ namespace hx {
 
 static inline bool is_p32(const hx_map* m) { return m->key_bytes == 4; }
 static inline uint64_t pair_bytes(const hx_map* m) { return is_p32(m) ? 8 : 16; }
+static inline unsigned key_bytes(const hx_map* m) { return is_p32(m) ? 4u : 8u; }
 static inline uint64_t nslots(const hx_map* m) { return 1ull << m->sp; }
 
 // Automatic probe policy (tune.group == 0), from GB300 sweeps over
@@ -760,6 +761,7 @@ static hx_status extract(hx_map* m, const hx_pred* pred, void* d_out, uint64_t c
   if (!valid_map(m) || !pred) return HX_ERR_INVALID_ARG;
   if (pred->op > HX_PRED_NOT_HOME || (pred->op == HX_PRED_MOD_LT && pred->a == 0)) return HX_ERR_INVALID_ARG;
   if (capacity && !d_out) return HX_ERR_INVALID_ARG;
+  if (misaligned(d_out, KEYS ? key_bytes(m) : pair_bytes(m))) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   std::lock_guard<std::mutex> g(m->mu);
   const uint64_t n = nslots(m);
@@ -854,6 +856,7 @@ hx_status hx_insert(hx_map* m, const void* d_keys, const void* d_vals, uint64_t 
   HX_CUDA(cudaMemsetAsync(&m->info->err, 0, sizeof(int), s));  // err = success (hashers.h:50)
   if (n == 0) return HX_OK;
   if (!d_keys || !d_vals) return HX_ERR_INVALID_ARG;
+  if (misaligned(d_keys, key_bytes(m)) || misaligned(d_vals, key_bytes(m))) return HX_ERR_INVALID_ARG;
   hx_status st = maybe_grow(m, n, target_lf, s);
   if (st != HX_OK) return st;
   HX_CUDA(cudaMemsetAsync(&m->info->err, 0, sizeof(int), s));
@@ -869,6 +872,7 @@ hx_status hx_insert_index(hx_map* m, const void* d_keys, uint64_t n, float targe
   HX_CUDA(cudaMemsetAsync(&m->info->err, 0, sizeof(int), s));
   if (n == 0) return HX_OK;
   if (!d_keys) return HX_ERR_INVALID_ARG;
+  if (misaligned(d_keys, key_bytes(m))) return HX_ERR_INVALID_ARG;
   hx_status st = maybe_grow(m, n, target_lf, s);
   if (st != HX_OK) return st;
   HX_CUDA(cudaMemsetAsync(&m->info->err, 0, sizeof(int), s));
@@ -884,6 +888,7 @@ hx_status hx_insert_pairs(hx_map* m, const void* d_pairs, uint64_t n, float targ
   HX_CUDA(cudaMemsetAsync(&m->info->err, 0, sizeof(int), s));
   if (n == 0) return HX_OK;
   if (!d_pairs) return HX_ERR_INVALID_ARG;
+  if (misaligned(d_pairs, pair_bytes(m))) return HX_ERR_INVALID_ARG;
   hx_status st = maybe_grow(m, n, target_lf, s);
   if (st != HX_OK) return st;
   HX_CUDA(cudaMemsetAsync(&m->info->err, 0, sizeof(int), s));
@@ -897,6 +902,7 @@ hx_status hx_retrieve(hx_map* m, const void* d_keys, void* d_vals, uint64_t n, h
   if (!valid_map(m)) return HX_ERR_INVALID_ARG;
   if (n == 0) return HX_OK;
   if (!d_keys || !d_vals) return HX_ERR_INVALID_ARG;
+  if (misaligned(d_keys, key_bytes(m)) || misaligned(d_vals, key_bytes(m))) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   return is_p32(m) ? launch_find<P32, false>(m, d_keys, d_vals, nullptr, n, s)
                    : launch_find<P64, false>(m, d_keys, d_vals, nullptr, n, s);
@@ -907,6 +913,7 @@ hx_status hx_retrieve_pairs(hx_map* m, void* d_pairs, uint64_t n, hx_stream stre
   if (!valid_map(m)) return HX_ERR_INVALID_ARG;
   if (n == 0) return HX_OK;
   if (!d_pairs) return HX_ERR_INVALID_ARG;
+  if (misaligned(d_pairs, pair_bytes(m))) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   return is_p32(m) ? launch_find<P32, false>(m, nullptr, nullptr, d_pairs, n, s)
                    : launch_find<P64, false>(m, nullptr, nullptr, d_pairs, n, s);
@@ -917,6 +924,7 @@ hx_status hx_erase(hx_map* m, const void* d_keys, uint64_t n, hx_stream stream) 
   if (!valid_map(m)) return HX_ERR_INVALID_ARG;
   if (n == 0) return HX_OK;
   if (!d_keys) return HX_ERR_INVALID_ARG;
+  if (misaligned(d_keys, key_bytes(m))) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   return is_p32(m) ? launch_find<P32, true>(m, d_keys, nullptr, nullptr, n, s)
                    : launch_find<P64, true>(m, d_keys, nullptr, nullptr, n, s);

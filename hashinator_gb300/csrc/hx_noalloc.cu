@@ -101,6 +101,7 @@ extern "C" hx_status hx_exclusive_scan_u32_noalloc(const uint32_t* d_in, uint32_
   HX_RANGE("hx_exclusive_scan_u32_noalloc");
   if (n == 0) return HX_OK;
   if (!d_in || !d_out) return HX_ERR_INVALID_ARG;
+  if (misaligned(d_in, 4) || misaligned(d_out, 4)) return HX_ERR_INVALID_ARG;
   if (n > HX_NOALLOC_SCAN_MAX_N) return HX_ERR_INVALID_ARG;  // beyond the fixed scratch: nothing launched
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int dev = 0;

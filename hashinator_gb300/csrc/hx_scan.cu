@@ -205,6 +205,7 @@ hx_status hx_exclusive_scan_u32(const uint32_t* d_in, uint32_t* d_out, uint64_t 
   HX_RANGE("hx_exclusive_scan_u32");
   if (n == 0) return HX_OK;
   if (!d_in || !d_out) return HX_ERR_INVALID_ARG;
+  if (misaligned(d_in, 4) || misaligned(d_out, 4)) return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const uint64_t tiles = scan_tiles(n);
   if (tiles > 0xFFFFFFFFull) return HX_ERR_INVALID_ARG;
@@ -223,6 +224,9 @@ hx_status hx_copy_if(const void* d_in, void* d_out, uint64_t n, int elem_bytes, 
   if (pred->op == HX_PRED_MOD_LT && pred->a == 0) return HX_ERR_INVALID_ARG;
   if (pred->op > HX_PRED_NOT_HOME) return HX_ERR_INVALID_ARG;
   if (pred->op == HX_PRED_NOT_HOME) return HX_ERR_INVALID_ARG;  // needs a map: hx_extract_pattern
+  if ((elem_bytes == 4 || elem_bytes == 8 || elem_bytes == 16) &&
+      (misaligned(d_in, (unsigned)elem_bytes) || misaligned(d_out, (unsigned)elem_bytes)))
+    return HX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   switch (elem_bytes) {
     case 4:

@@ -231,12 +231,15 @@ __global__ void __launch_bounds__(BLOCK) k_scan_u32(const uint32_t* in, uint32_t
 // instead of a switch (and a division) per element.
 enum : int { PK_GENERIC = 0, PK_MOD_LT32 = 1, PK_MASK_EQ = 2, PK_VALID = 3, PK_MOD_LT_THRESH = 4 };
 
-// (x mod d) < s for 32-bit x and 2 <= d <= 2^31, 0 < s < d, with one 64-bit
-// multiply and a compare, derived from the direct-remainder method cited
-// below: with M = ceil(2^64 / d), write x = q*d + r and M*d = 2^64 + e
-// (0 <= e < d); then M*x mod 2^64 = r*M + q*e without wrapping, and because
-// q*e < 2^32 < M, r < s exactly when M*x mod 2^64 < s*M. The host computes
-// the threshold s*M (below 2^64, as s < d).
+// (x mod d) < s for 32-bit x and 2 <= d <= 2^31, 0 < s < d, from the high
+// 32 bits of one product, derived from the direct-remainder method cited
+// below: with M = ceil(2^64 / d) (at least 2^33), write x = q*d + r and
+// M*d = 2^64 + e (0 <= e < d); then L = M*x mod 2^64 = r*M + q*e without
+// wrapping, with 0 <= q*e < 2^32. If r >= s, L >= s*M. If r < s,
+// L < (s-1)*M + 2^32 <= s*M - 2^32. So r < s exactly when
+// floor(L / 2^32) < floor(s*M / 2^32), and floor(L / 2^32) is
+// umulhi(M_lo, x) + M_hi*x mod 2^32: two 32-bit multiplies and a compare.
+// The host computes the threshold floor(s*M / 2^32) (s*M < 2^64, as s < d).
 __host__ __device__ inline bool mod_lt_thresh_ok(uint64_t d, uint64_t s) {
   return d >= 2 && d <= (1ull << 31) && s > 0 && s < d;
 }
@@ -325,10 +328,13 @@ __device__ __forceinline__ O project(const T& x) {
 // clean_tombstones mode (CLEAN): the input is the bucket array itself. Every
 // TOMBSTONE bucket and every selected (moved) bucket is rewritten to
 // (EMPTY, 0) after it has been read, the last tile takes the moved count off
-// fill, and the whole pass is skipped when *skip is set. Reading a home
-// bucket that another CTA rewrites at the same time cannot change a decision:
-// a key Y is "not home" iff bucket[home(Y)] holds a key other than Y, and that
-// bucket only ever changes between keys other than Y and EMPTY.
+// fill, and the whole pass is skipped when *skip is set. The
+// phase-partitioned kernel decides "not home" from the bucket's index
+// (home(Y) != i) and reads no other bucket. The look-back kernel reads the
+// home bucket; one that another CTA rewrites at the same time cannot change
+// its decision: a key Y is "not home" iff bucket[home(Y)] holds a key other
+// than Y, and that bucket only ever changes between keys other than Y and
+// EMPTY.
 struct CleanArgs {
   const unsigned* skip;
   unsigned long long* fill;
@@ -555,14 +561,13 @@ inline cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint64_t n, vo
 // The predicate of a compaction for the phase-partitioned kernel: one
 // compiled predicate kind (PK_*), and in clean_tombstones mode (CLEAN) the
 // rewrite of every TOMBSTONE and every selected bucket to (EMPTY, 0) after
-// it has been read (see CleanArgs for why concurrent reads of home buckets
-// are safe).
+// it has been read (see CleanArgs).
 template <class T, int PK, bool CLEAN>
 struct PredSel {
   hx_pred pr;
   uint64_t magic;
   typename ElemOps<T>::Ctx ctx;
-  uint64_t thresh = 0;  // PK_MOD_LT_THRESH: s * magic
+  uint64_t thresh = 0;  // PK_MOD_LT_THRESH: floor(s * magic / 2^32)
   static constexpr bool kRewrites = CLEAN;
   // generic pair rules may be HX_PRED_NOT_HOME, which compares a bucket's
   // index with its key's home bucket
@@ -576,7 +581,8 @@ struct PredSel {
       uint32_t f;
       if constexpr (std::is_same<T, uint32_t>::value) f = x;
       else f = (uint32_t)(pr.field == HX_FIELD_VALUE ? x.second : x.first);
-      bool r = magic * (uint64_t)f < thresh;
+      const uint32_t hi = __umulhi((uint32_t)magic, f) + (uint32_t)(magic >> 32) * f;
+      bool r = hi < (uint32_t)thresh;
       if constexpr (!std::is_same<T, uint32_t>::value) {
         using Tr = PairTraits<T>;
         if ((pr.flags & HX_PRED_SKIP_SENTINELS) && (x.first == Tr::EMPTY || x.first == Tr::TOMB)) r = false;
@@ -620,7 +626,7 @@ inline cudaError_t launch_compact(const T* in, O* out, uint64_t n, const hx_pred
         case PK_MOD_LT32:
           if (mod_lt_thresh_ok(pr.a, pr.b)) {
             const uint64_t m = fastmod_magic((uint32_t)pr.a);
-            return go(PredSel<T, PK_MOD_LT_THRESH, false>{pr, m, ctx, pr.b * m});
+            return go(PredSel<T, PK_MOD_LT_THRESH, false>{pr, m, ctx, (pr.b * m) >> 32});
           }
           return go(PredSel<T, PK_MOD_LT32, false>{pr, fastmod_magic((uint32_t)pr.a), ctx});
         case PK_MASK_EQ:

@@ -538,7 +538,8 @@ hx_status hx_server_submit(hx_server* sv, const hx_request* reqs, uint32_t count
   for (uint32_t i = 0; i < count; ++i) {
     const hx_request& r = reqs[i];
     if (r.map >= sv->maps.size() || r.op > SOP_ERASE || (r.n && !r.keys) || (r.op == SOP_INSERT && r.n && !r.vals) ||
-        (r.op == SOP_QUERY && r.n && !r.out))
+        (r.op == SOP_QUERY && r.n && !r.out) || misaligned(r.keys, (unsigned)sv->kb) ||
+        misaligned(r.vals, (unsigned)sv->kb) || misaligned(r.out, (unsigned)sv->kb))
       return HX_ERR_INVALID_ARG;
   }
   for (uint32_t i = 0; i < count; ++i) sv->queue.push_back(Pending{reqs[i], sv->seq++});

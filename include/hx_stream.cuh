@@ -34,8 +34,10 @@
 #include <stdint.h>
 #include <string.h>
 
-#include <atomic>
+#include <map>
+#include <mutex>
 #include <type_traits>
+#include <utility>
 
 namespace hxs {
 
@@ -126,8 +128,11 @@ constexpr int kR = HX_STREAM_R;
 constexpr int kStages = HX_STREAM_STAGES;
 constexpr int kDefer = HX_STREAM_DEFER;
 static_assert(kDefer >= 1 && kDefer < kStages, "a stage must be free to load while D phases wait");
-// Count slots per CTA: a CTA overwrites the slot of phase p - kSlots only
-// after every CTA has read it (see the kernel), which needs 2 * D + 2 slots.
+// Count slots per CTA. In phase p a CTA publishes its count of p, then
+// reads every CTA's count of p - D; so when it publishes p it has read every
+// count of p - 1 - D, every CTA has published p - 1 - D, and every CTA has
+// therefore read every count of the phases up to p - 2 - 2D. The row of
+// phase p is the row of phase p - kSlots, so kSlots = 2D + 2.
 constexpr int kSlots = 2 * kDefer + 2;
 constexpr int kMaxGrid = 1024;  // CTAs at most (GB300: 152 SMs x 1-2 CTAs); a larger device runs 1024
 constexpr int kSlotLoads = (kMaxGrid + kBlock - 1) / kBlock;  // count slots each thread reads per phase
@@ -223,7 +228,7 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
   __shared__ __align__(8) uint64_t s_bar[kStages];
   __shared__ unsigned s_warp[WARPS];
   __shared__ unsigned s_cnt[kStages];
-  __shared__ unsigned long long s_red[2][WARPS];
+  __shared__ uint2 s_red[WARPS];  // per warp: (count before this CTA, phase total), both < 2^32
   __shared__ int s_abort;
 
   // Device-side inputs: the same values for every CTA, so every CTA runs the
@@ -233,15 +238,15 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned G = gridDim.x, b = blockIdx.x;
   const uint64_t full_slices = n / SE;  // slices wholly inside [0, n)
-  const unsigned long long phases = ((n + SE - 1) / SE + G - 1) / G;
+  const unsigned phases = (unsigned)(((n + SE - 1) / SE + G - 1) / G);  // below 2^32 - kDefer (launch)
   unsigned pend = 0;                    // thread 0: stages with a bulk copy not yet seen complete
   unsigned par = 0;                     // parity of the next wait, bit per stage
 
   // Fill stage st with the slice of phase p (thread 0): a whole slice by one
   // bulk copy; the ragged last slice and slices past n are read later with
   // plain loads, so their barrier phase completes with no bytes.
-  auto issue = [&](int st, unsigned long long p) {
-    const uint64_t t = p * G + b;
+  auto issue = [&](int st, unsigned p) {
+    const uint64_t t = (uint64_t)p * G + b;
     if (t < full_slices) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier reads of the stage come first
       mbar_expect_tx(&s_bar[st], kSliceBytes);
@@ -258,17 +263,21 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
   }
   __syncthreads();
   if (threadIdx.x == 0)
-    for (int s = 0; s < kStages && (unsigned long long)s < phases; ++s) issue(s, s);
+    for (int s = 0; s < kStages && (unsigned)s < phases; ++s) issue(s, s);
 
   // result count (or sum) of the phases already written, after any elements placed before this pass
   unsigned long long base = done.base_from ? *done.base_from : 0ull;
   bool failed = false;
-  for (unsigned long long p = 0; p < phases + kDefer; ++p) {
+  // stage and count-slot row of phase p (pass 1) and of phase p - kDefer
+  // (pass 2), advanced by one each phase instead of computed by division
+  unsigned st1 = 0, st2 = 0, sl1 = 0, sl2 = 0;
+  auto next = [](unsigned& i, unsigned m) { i = i + 1 == m ? 0u : i + 1; };
+  for (unsigned p = 0; p < phases + kDefer; ++p) {
     // The count slots that pass 2 reads below were published kDefer phases
     // ago: load them now, so that their latency overlaps pass 1.
     unsigned long long pv[kSlotLoads];
-    if (p >= (unsigned long long)kDefer) {
-      const unsigned long long* row = sc.slots + ((p - kDefer) % kSlots) * G;
+    if (p >= (unsigned)kDefer) {
+      const unsigned long long* row = sc.slots + sl2 * G;
 #pragma unroll
       for (int k = 0; k < kSlotLoads; ++k) {
         const unsigned c = threadIdx.x + k * kBlock;
@@ -277,13 +286,13 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
     }
     // ---- pass 1: phase p -------------------------------------------------
     if (p < phases) {
-      const int st = (int)(p % kStages);
+      const unsigned st = st1;
       const bool ok = mbar_wait(&s_bar[st], (par >> st) & 1u);
       if (ok) {  // a failed wait leaves par and pend as they were, for the drain below
         par ^= 1u << st;
         pend &= ~(1u << st);
       }
-      const uint64_t t = p * G + b;
+      const uint64_t t = (uint64_t)p * G + b;
       const bool whole = t < full_slices;
       const uint64_t e0 = t * SE;
       T x[kR][E];
@@ -386,7 +395,7 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
         if (lane == 31) {
           s_cnt[st] = wincl;
           // publish this CTA's count (or sum, mod 2^32) of phase p, tagged with p + 1
-          st_relaxed(sc.slots + (p % kSlots) * G + b, ((p + 1) << 32) | wincl);
+          st_relaxed(sc.slots + sl1 * G + b, ((unsigned long long)(p + 1) << 32) | wincl);
         }
       }
       __syncthreads();
@@ -411,22 +420,24 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
       }
     }
     // ---- pass 2: phase p - D ---------------------------------------------
-    if (p >= (unsigned long long)kDefer) {
-      const unsigned long long q = p - kDefer;
-      const int st = (int)(q % kStages);
-      // every CTA's count of phase q: the sum over CTAs before this one, and the total
-      unsigned long long before = 0, total = 0;
+    if (p >= (unsigned)kDefer) {
+      const unsigned q = p - kDefer;
+      const unsigned st = st2;
+      // Every CTA's count of phase q: the sum over CTAs before this one, and
+      // the total. A phase holds at most kMaxGrid slices of at most 2^14
+      // elements, so both fit 32 bits (the scan's sums are taken mod 2^32).
+      unsigned before = 0, total = 0;
       bool ok = true;
 #pragma unroll
       for (int k = 0; k < kSlotLoads; ++k) {
         const unsigned c = threadIdx.x + k * kBlock;
         if (c >= G) break;
-        const unsigned long long* slot = sc.slots + (q % kSlots) * G + c;
+        const unsigned long long* slot = sc.slots + sl2 * G + c;
         unsigned long long v = pv[k];
-        if ((v >> 32) != q + 1) {
+        if ((unsigned)(v >> 32) != q + 1) {
           const unsigned long long t0 = globaltimer();
           unsigned i = 0;
-          while ((v >> 32) != q + 1) {
+          while ((unsigned)(v >> 32) != q + 1) {
             if ((++i & 63) == 0) {
               if (ld_relaxed_u32(sc.error) || globaltimer() - t0 > kWaitNs) {
                 ok = false;
@@ -438,18 +449,19 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
           }
           if (!ok) break;
         }
-        const unsigned long long cnt = v & 0xffffffffull;
+        const unsigned cnt = (unsigned)v;
         total += cnt;
         if (c < b) before += cnt;
       }
+      // only the warps that read a slot reduce; the others hold zeros
+      const unsigned nw = G >= (unsigned)kBlock ? (unsigned)WARPS : (G + 31) / 32;
+      if ((unsigned)warp < nw) {
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        before += __shfl_xor_sync(0xffffffffu, before, o);
-        total += __shfl_xor_sync(0xffffffffu, total, o);
-      }
-      if (lane == 0) {
-        s_red[0][warp] = before;
-        s_red[1][warp] = total;
+        for (int o = 16; o > 0; o >>= 1) {
+          before += __shfl_xor_sync(0xffffffffu, before, o);
+          total += __shfl_xor_sync(0xffffffffu, total, o);
+        }
+        if (lane == 0) s_red[warp] = make_uint2(before, total);
       }
       if (__syncthreads_or(!ok)) {
         failed = true;
@@ -457,14 +469,14 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
       }
       before = 0;
       total = 0;
-#pragma unroll
-      for (int w = 0; w < WARPS; ++w) {
-        before += s_red[0][w];
-        total += s_red[1][w];
+      for (unsigned w = 0; w < nw; ++w) {
+        const uint2 r = s_red[w];
+        before += r.x;
+        total += r.y;
       }
       const unsigned long long prefix = base + before;
       const uint4* stage = s_stage + (size_t)st * SU4;
-      const uint64_t t = q * G + b;
+      const uint64_t t = (uint64_t)q * G + b;
       if constexpr (SCAN) {
         const uint64_t e0 = t * SE;
         const unsigned add = (unsigned)prefix;
@@ -494,7 +506,11 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
       base += total;
       __syncthreads();  // stage st is written out
       if (threadIdx.x == 0 && q + kStages < phases) issue(st, q + kStages);
+      next(st2, kStages);
+      next(sl2, kSlots);
     }
+    next(st1, kStages);
+    next(sl1, kSlots);
   }
   if (failed) {
     if (threadIdx.x == 0) {
@@ -515,31 +531,45 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
 // ---- host side -------------------------------------------------------------
 inline size_t smem_bytes() { return (size_t)kStages * kSliceBytes; }
 
-// Co-resident CTAs of one instantiation on the current device (SMs x CTAs
-// per SM, at most kMaxGrid), queried once per instantiation and device.
-template <class T, class O, class Sel, bool SCAN>
-inline cudaError_t resident_grid(unsigned* grid) {
-  auto kern = k_stream<T, O, Sel, SCAN>;
-  static std::atomic<int> cache[64];
+// Co-resident CTAs of one kernel on the current device (SMs x CTAs per SM,
+// at most kMaxGrid), with the kernel's shared-memory limit raised first.
+// The limit is raised on every call (cheap, and it survives a device reset
+// that would drop it); the occupancy query runs once per kernel and device.
+// The cache is keyed by the kernel's host-side address, not by its template
+// arguments alone: a kernel template instantiated in several translation
+// units (libhx's, a caller's, the no-allocation scan's) is a separate
+// function in each, while a static of an inline function is one object
+// shared by all of them.
+template <class Kern>
+inline cudaError_t resident_grid(Kern kern, unsigned* grid) {
+  const size_t smem = smem_bytes();
+  cudaError_t e = cudaSuccess;
+  if (smem > 48 * 1024) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
   int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  int g = (dev >= 0 && dev < 64) ? cache[dev].load(std::memory_order_relaxed) : 0;
-  if (g == 0) {
-    const size_t smem = smem_bytes();
-    if (smem > 48 * 1024) {
-      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, unsigned> cache;
+  const auto key = std::make_pair(reinterpret_cast<const void*>(kern), dev);
+  {
+    std::lock_guard<std::mutex> g(mu);
+    const auto it = cache.find(key);
+    if (it != cache.end()) {
+      *grid = it->second;
+      return cudaSuccess;
     }
-    int per_sm = 0, sms = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, smem);
-    if (e != cudaSuccess) return e;
-    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    g = per_sm * sms;
-    if (g < 1) return cudaErrorInvalidConfiguration;
-    if (g > kMaxGrid) g = kMaxGrid;
-    if (dev >= 0 && dev < 64) cache[dev].store(g, std::memory_order_relaxed);  // every writer stores the same
+  }
+  int per_sm = 0, sms = 0;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, smem)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  long g = (long)per_sm * sms;
+  if (g < 1) return cudaErrorInvalidConfiguration;
+  if (g > kMaxGrid) g = kMaxGrid;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    cache[key] = (unsigned)g;
   }
   *grid = (unsigned)g;
   return cudaSuccess;
@@ -554,11 +584,12 @@ inline cudaError_t launch(const T* in, O* out, uint64_t n, const Sel& sel, uint6
                           void* scratch, cudaStream_t s) {
   auto kern = k_stream<T, O, Sel, SCAN>;
   unsigned grid = 0;
-  cudaError_t e = resident_grid<T, O, Sel, SCAN>(&grid);
+  cudaError_t e = resident_grid(kern, &grid);
   if (e != cudaSuccess) return e;
   constexpr uint64_t SE = (uint64_t)kBlock * kR * (16 / sizeof(T));
   const uint64_t slices = (n + SE - 1) / SE;
   if (slices < grid) grid = (unsigned)slices;
+  if (slices / grid >= 0xffff0000ull) return cudaErrorInvalidValue;  // phases are counted in 32 bits
   e = cudaMemsetAsync(scratch, 0, scratch_bytes_used(grid), s);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};

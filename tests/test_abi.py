@@ -132,3 +132,32 @@ def test_header_is_plain_c(tmp_path):
     r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", str(ROOT / "include"),
                         "-c", str(src), "-o", str(tmp_path / "use_hx.o")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_misaligned_device_arrays_are_rejected(hx):
+    """Device arrays must start at a multiple of their element size (4-byte words, 8- or 16-byte pairs): a
+    misaligned pointer is rejected before any device work. Every call here must be rejected, so the fake
+    pointers are never dereferenced; the aligned control calls fail later, on the scratch check, which shows
+    that the alignment check is what rejected the others."""
+    lib = hx.lib()
+    p = hx.Pred.mod_lt(100, 50).c()
+    n = 5000
+    ok = 1 << 20
+    for elem in (4, 8, 16):
+        for off in range(1, elem):
+            bad = ctypes.c_void_p(ok + off)
+            good = ctypes.c_void_p(ok)
+            assert lib.hx_copy_if(bad, good, n, elem, ctypes.byref(p), n, None, None, good, 1 << 20, None) == \
+                hx.HX_ERR_INVALID_ARG
+            assert lib.hx_copy_if(good, bad, n, elem, ctypes.byref(p), n, None, None, good, 1 << 20, None) == \
+                hx.HX_ERR_INVALID_ARG
+    for off in (1, 2, 3):
+        bad, good = ctypes.c_void_p(ok + off), ctypes.c_void_p(ok)
+        assert lib.hx_exclusive_scan_u32(bad, good, n, good, 1 << 20, None) == hx.HX_ERR_INVALID_ARG
+        assert lib.hx_exclusive_scan_u32(good, bad, n, good, 1 << 20, None) == hx.HX_ERR_INVALID_ARG
+        assert lib.hx_exclusive_scan_u32_noalloc(bad, good, n, None) == hx.HX_ERR_INVALID_ARG
+        assert lib.hx_exclusive_scan_u32_noalloc(good, bad, n, None) == hx.HX_ERR_INVALID_ARG
+    # controls: aligned, with an undersized caller scratch, rejected by the scratch check instead
+    good = ctypes.c_void_p(ok)
+    assert lib.hx_copy_if(good, good, n, 8, ctypes.byref(p), n, None, None, good, 16, None) == hx.HX_ERR_INVALID_ARG
+    assert lib.hx_exclusive_scan_u32(good, good, n, good, 16, None) == hx.HX_ERR_INVALID_ARG

@@ -2,10 +2,12 @@
 with Python integers: the direct-remainder method used by the compaction's
 `x % d < s` predicate (hx_scan.cuh fastmod_magic / fastmod_u32: with
 M = floor((2^64 - 1) / d) + 1 mod 2^64, x mod d is the high 64 bits of
-((M * x) mod 2^64) * d, for 32-bit x and 1 <= d < 2^32), the one-multiply
-threshold form of `x % d < s` (hx_scan.cuh PK_MOD_LT_THRESH: for 2 <= d <=
-2^31 and 0 < s < d, (x mod d) < s exactly when (M * x) mod 2^64 < s * M), and
-the build flags (sm_103a only, with line info)."""
+((M * x) mod 2^64) * d, for 32-bit x and 1 <= d < 2^32), the threshold
+form of `x % d < s` (hx_scan.cuh PK_MOD_LT_THRESH: for 2 <= d <= 2^31 and
+0 < s < d, (x mod d) < s exactly when the high 32 bits of (M * x) mod 2^64
+are below the high 32 bits of s * M, the left side computed as
+umulhi(M_lo, x) + M_hi * x mod 2^32, as the kernel does), and the build flags
+(sm_103a only, with line info)."""
 import random
 
 import pytest
@@ -48,8 +50,11 @@ def thresh_ok(d: int, s: int) -> bool:  # mod_lt_thresh_ok in hx_scan.cuh
 def mod_lt_by_threshold(x: int, d: int, s: int) -> bool:
     magic = (M64 // d + 1) & M64
     t = s * magic
-    assert t <= M64  # the threshold fits 64 bits
-    return ((magic * x) & M64) < t
+    assert t <= M64  # s * M fits 64 bits
+    m_lo, m_hi = magic & 0xFFFFFFFF, magic >> 32
+    hi = (((m_lo * x) >> 32) + m_hi * x) & 0xFFFFFFFF  # umulhi(M_lo, x) + M_hi * x, in 32 bits
+    assert hi == ((magic * x) & M64) >> 32
+    return hi < (t >> 32)
 
 
 @pytest.mark.parametrize("d", [d for d in DIVISORS if 2 <= d <= (1 << 31)])

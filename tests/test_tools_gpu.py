@@ -118,6 +118,46 @@ def test_copy_if_capacity_and_device_count(hx, oracle_mod):
     assert int(dc.item()) == 5000
 
 
+@pytest.mark.parametrize("eb", [4, 8, 16])
+@pytest.mark.parametrize("off", [0, 4, 8, 12])
+def test_copy_if_output_offsets_and_capacity_cuts(hx, eb, off):
+    """The compaction stores each CTA's run with 16-byte stores between
+    element-by-element edges: outputs that start 4, 8 or 12 bytes past a
+    16-byte boundary, and capacities that cut a run anywhere. The bytes before
+    the output and after the last stored element stay as they were. An output
+    that is not a multiple of the element size from 16-byte alignment (8-byte
+    pairs at 4 bytes, 16-byte pairs at 4, 8, 12) is rejected before any
+    device work."""
+    import torch
+    n = (1 << 20) + 12345
+    dt = np.uint32 if eb in (4, 8) else np.uint64
+    words = n * eb // np.dtype(dt).itemsize
+    x = np.random.default_rng(eb * 100 + off).integers(0, np.iinfo(dt).max, size=words, dtype=dt, endpoint=True)
+    rows = x.reshape(n, -1)
+    key = rows[:, 0]
+    sel = (key % dt(3)) < dt(2)  # about two thirds selected: long runs per CTA
+    want = rows[sel].reshape(-1)
+    pred = hx.Pred(hx.PRED_MOD_LT, hx.FIELD_ELEM if eb == 4 else hx.FIELD_KEY, 3, 2)
+    d_in = to_dev(x)
+    total = len(want) * np.dtype(dt).itemsize
+    buf = torch.full((total + 64,), 0x5A, dtype=torch.uint8, device="cuda")
+    base = buf.data_ptr() + off
+    if off % eb:
+        with pytest.raises(hx.HXError):
+            hx.tools.copy_if(d_in, base, pred, elem_bytes=eb, n=n, capacity=len(want))
+        assert (buf.cpu().numpy() == 0x5A).all()
+        return
+    for cap in (int(sel.sum()), int(sel.sum()) // 3 + 1, 1, 0, 16384 * 5 + 3):
+        buf.fill_(0x5A)
+        c = hx.tools.copy_if(d_in, base, pred, elem_bytes=eb, n=n, capacity=cap)
+        assert c == int(sel.sum())
+        got = buf.cpu().numpy()
+        kept = min(cap, c) * eb
+        assert (got[:off] == 0x5A).all()
+        np.testing.assert_array_equal(got[off:off + kept], want.view(np.uint8)[:kept])
+        assert (got[off + kept:] == 0x5A).all()
+
+
 def test_copy_if_empty_input(hx):
     import torch
     e = torch.zeros(0, dtype=torch.int32, device="cuda")

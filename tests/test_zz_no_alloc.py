@@ -40,8 +40,10 @@ def _both(hx, x: np.ndarray, stream: int):
     want = torch.zeros_like(d_in)
     got = torch.full_like(d_in, 0x5A5A5A5A)
     n = len(x)
-    assert lib.hx_exclusive_scan_u32(d_in.data_ptr(), want.data_ptr(), n, None, 0, stream) == 0
-    assert noalloc(d_in.data_ptr(), got.data_ptr(), n, stream) == 0
+    st = lib.hx_exclusive_scan_u32(d_in.data_ptr(), want.data_ptr(), n, None, 0, stream)
+    assert st == 0, f"status {st}, cudaError {lib.hx_last_cuda_error()}"
+    st = noalloc(d_in.data_ptr(), got.data_ptr(), n, stream)
+    assert st == 0, f"status {st}, cudaError {lib.hx_last_cuda_error()}"
     torch.cuda.synchronize()
     return from_dev(got, np.uint32), from_dev(want, np.uint32)
 
