@@ -3,7 +3,10 @@
  *
  * Every entry point is `extern "C"`, takes plain pointers and sizes and
  * returns an hx_status. Device pointers must be device-accessible memory
- * (cudaMalloc, cudaMallocAsync or managed). Streams are passed as opaque
+ * (cudaMalloc, cudaMallocAsync or managed), and an array of elements of
+ * k bytes (4-byte keys or words, 8-byte keys, 8- or 16-byte pairs) must start
+ * at a multiple of k: a misaligned array is rejected with
+ * HX_ERR_INVALID_ARG before any device work. Streams are passed as opaque
  * `hx_stream` values (a cudaStream_t; NULL = the legacy default stream).
  *
  * Calls are stream-ordered and asynchronous unless their comment says they
