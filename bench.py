@@ -994,20 +994,24 @@ def run_ours(args):
         h_vals = torch.from_numpy(vals.view(np.int32)).pin_memory()
         h_q = torch.from_numpy(q.view(np.int32)).pin_memory()
         h_out = torch.empty(n, dtype=torch.int32).pin_memory()
-        # Two device buffer sets and separate upload / download streams: step k+1's
-        # uploads run while step k's kernels do; a set is reused only after the
+        # Several device buffer sets and separate upload / download streams: later
+        # steps' uploads run while step k's kernels do; a set is reused only after the
         # step that last used it has consumed its inputs and downloaded its results.
+        # With two sets, step k's uploads wait for step k-2's downloads and end just
+        # as step k-1's kernels do; a third set takes that wait off the path.
         h2d = torch.cuda.Stream(device=dev)
         d2h = torch.cuda.Stream(device=dev)
-        bufs = [(d_keys, d_vals, d_q, d_out),
-                (torch.empty_like(d_keys), torch.empty_like(d_vals), torch.empty_like(d_q), d_out.clone())]
-        free = [None, None]
+        nsets = max(2, args.e2e_sets)
+        bufs = [(d_keys, d_vals, d_q, d_out)] + [
+            (torch.empty_like(d_keys), torch.empty_like(d_vals), torch.empty_like(d_q), d_out.clone())
+            for _ in range(nsets - 1)]
+        free = [None] * nsets
         chunks = args.e2e_chunks
         bounds = [(c * n // chunks, (c + 1) * n // chunks) for c in range(chunks)]
         step_no = [0]
 
         def e2e_step():
-            k = step_no[0] % 2
+            k = step_no[0] % nsets
             step_no[0] += 1
             bk, bv, bq, bo = bufs[k]
             kv_ready, q_ready = [], []
@@ -1069,7 +1073,7 @@ def run_ours(args):
         h2d.wait_event(s0)  # the first uploads start inside the timed region
         for _ in range(args.steps):
             e2e_step()
-        stream.wait_event(free[(step_no[0] - 1) % 2])  # the timed region ends with the last results on the host
+        stream.wait_event(free[(step_no[0] - 1) % nsets])  # the timed region ends with the last results on the host
         s1.record(stream)
         torch.cuda.synchronize()
         e_el = max_over_ranks(s0.elapsed_time(s1) / 1e3, dev)
@@ -1079,7 +1083,7 @@ def run_ours(args):
                "h2d_bytes_per_step": 3 * n * width, "d2h_bytes_per_step": n * width,
                "ms_per_step": round(e_el / args.steps * 1e3, 3), "chunks": chunks,
                "api": "hashinator_gb300.Hashmap (libhx C ABI); upload, compute and download streams overlapped "
-                      "across steps with two device buffer sets",
+                      f"across steps with {nsets} device buffer sets",
                "host_link": link,
                "link_bound_ms_per_step": round(3 * n * width / (link["h2d_GB_s"] * 1e9) * 1e3
                                                + n * width / (link["d2h_GB_s"] * 1e9) * 1e3, 3)}
@@ -1167,14 +1171,15 @@ def run_case(args):
     """One kernel case on its own, for an ncu capture. --case-kind map: a table of 2^case_log_buckets buckets,
     the case_lf share of them inserted (case_reps times, each after a clear), then the same number of 50%-hit
     queries (case_reps times). --case-kind copy_if / scan: 2^case_log_n uniform u32, copy_if with
-    (x % 100) < case_s, or the exclusive scan of x & 15, case_reps times. Prints one JSON line with the
-    per-launch times."""
+    (x % 100) < case_s, or the exclusive scan of x & 15, case_reps times. --case-kind clean: the map case's
+    table with 30% of its keys erased, then one clean_tombstones (after a clean with no tombstones has sized
+    the map's scratch). Prints one JSON line with the per-launch times."""
     import torch
     import hashinator_gb300 as hx
     from hashinator_gb300 import workloads
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
-    if args.case_kind != "map":
+    if args.case_kind in ("copy_if", "scan"):
         n = 1 << args.case_log_n
         g = torch.Generator(device=dev).manual_seed(7)
         x = torch.randint(0, 2**31 - 1, (n,), dtype=torch.int64, device=dev, generator=g)
@@ -1208,6 +1213,25 @@ def run_case(args):
     o = torch.empty_like(dq)
     stream = torch.cuda.Stream(device=dev)
     m = hx.Hashmap(sp, w, stream=stream)
+    if args.case_kind == "clean":
+        rng = np.random.default_rng(50 + w)
+        de = torch.from_numpy(np.ascontiguousarray(keys[workloads.affine_sample(n, int(0.3 * n), rng)]).view(sig))
+        de = de.to(dev)
+        m.insert(dk, dv, target_lf=0.0, stream=stream)
+        m.clean_tombstones(stream=stream)  # no tombstones yet: sizes the scratch, runs no pass
+        m.erase(de, stream=stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        m.clean_tombstones(stream=stream)  # once: a second clean finds no tombstones
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_c = e0.elapsed_time(e1) / 1e3
+        inf = m.info(stream=stream)
+        print(json.dumps({"case": f"clean_tombstones u{8 * w} 2^{sp} buckets LF {args.case_lf}, 30% erased",
+                          "clean_ms": round(t_c * 1e3, 3), "moved": int(inf.last_clean_moved),
+                          "fill": int(inf.fill), "tombstones": int(inf.tombstone_counter)}), flush=True)
+        m.close()
+        return 0
     t_clear = _ev_time(stream, lambda: m.clear(stream=stream), reps=args.case_reps)
     t_ins = _ev_time(stream, lambda: (m.clear(stream=stream), m.insert(dk, dv, target_lf=0.0, stream=stream)),
                      reps=args.case_reps)
@@ -1230,7 +1254,8 @@ def main():
     ap.add_argument("--group", type=int, default=0, help="probe-group width (0 = library default)")
     ap.add_argument("--log-keys", type=int, default=26, help="log2 of the key count (table: twice as many buckets)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--e2e-chunks", type=int, default=8)
+    ap.add_argument("--e2e-chunks", type=int, default=2)
+    ap.add_argument("--e2e-sets", type=int, default=3, help="device buffer sets the e2e pipeline rotates")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-maps", type=int, default=4096)
     ap.add_argument("--batched-tuning", type=int, nargs=3, metavar=("GROUP", "BLOCK", "TILE"),
@@ -1248,7 +1273,7 @@ def main():
     ap.add_argument("--case-lf", type=float, default=0.5)
     ap.add_argument("--case-log-buckets", type=int, default=27)
     ap.add_argument("--case-reps", type=int, default=1)
-    ap.add_argument("--case-kind", default="map", choices=["map", "copy_if", "scan"])
+    ap.add_argument("--case-kind", default="map", choices=["map", "copy_if", "scan", "clean"])
     ap.add_argument("--case-log-n", type=int, default=26)
     ap.add_argument("--case-s", type=int, default=1, help="copy_if selectivity in percent")
     args = ap.parse_args()
