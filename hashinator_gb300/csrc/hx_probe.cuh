@@ -465,24 +465,21 @@ __device__ __forceinline__ int insert_t1_win(P* __restrict__ table, int sp, type
   }
 }
 
-// One key into one table, thread-per-key: blind CAS at home, then probe.
+// The rest of a thread-per-key insert once its first blind CAS at home has
+// failed and left the bucket's content in (ek, ev): retry while the bucket is
+// EMPTY with a stale value (nine attempts in all), overwrite the value if the
+// bucket holds the key, else probe on.
 template <class P, int B>
-__device__ __forceinline__ void insert_one_t1(P* tab, int sp, typename PairTraits<P>::K key,
-                                                typename PairTraits<P>::V val, unsigned& ins, unsigned& maxd,
-                                                bool& fail) {
-  using K = typename PairTraits<P>::K;
-  using V = typename PairTraits<P>::V;
-  if (key == PairTraits<P>::EMPTY || key == PairTraits<P>::TOMB) return;
-  const uint32_t h = home_slot(key, sp);
-  K ek = PairTraits<P>::EMPTY;
-  V ev = 0;
-  for (int tries = 0; tries < 9; ++tries) {
+__device__ __forceinline__ void insert_t1_after_cas(P* tab, int sp, typename PairTraits<P>::K key,
+                                                    typename PairTraits<P>::V val, uint32_t h,
+                                                    typename PairTraits<P>::K ek, typename PairTraits<P>::V ev,
+                                                    unsigned& ins, unsigned& maxd, bool& fail) {
+  for (int tries = 1; tries < 9 && ek == PairTraits<P>::EMPTY; ++tries) {
     if (cas_pair(tab + h, ek, ev, key, val)) {
       ++ins;
       maxd = maxd > 1u ? maxd : 1u;
       return;
     }
-    if (ek != PairTraits<P>::EMPTY) break;  // taken (or EMPTY with a stale value: retry)
   }
   if (ek == key) {
     store_value(tab + h, val);
@@ -495,6 +492,69 @@ __device__ __forceinline__ void insert_one_t1(P* tab, int sp, typename PairTrait
     maxd = d1 > maxd ? d1 : maxd;
   } else if (r == PR_FAIL) {
     fail = true;
+  }
+}
+
+// One key into one table, thread-per-key: blind CAS at home, then probe.
+template <class P, int B>
+__device__ __forceinline__ void insert_one_t1(P* tab, int sp, typename PairTraits<P>::K key,
+                                                typename PairTraits<P>::V val, unsigned& ins, unsigned& maxd,
+                                                bool& fail) {
+  using K = typename PairTraits<P>::K;
+  using V = typename PairTraits<P>::V;
+  if (key == PairTraits<P>::EMPTY || key == PairTraits<P>::TOMB) return;
+  const uint32_t h = home_slot(key, sp);
+  K ek = PairTraits<P>::EMPTY;
+  V ev = 0;
+  if (cas_pair(tab + h, ek, ev, key, val)) {
+    ++ins;
+    maxd = maxd > 1u ? maxd : 1u;
+    return;
+  }
+  insert_t1_after_cas<P, B>(tab, sp, key, val, h, ek, ev, ins, maxd, fail);
+}
+
+// U keys per thread, elements first + u * stride (those below count), each
+// loaded by load(i, key, val): their first CASes at home are issued together,
+// so U atomics are in flight per thread, and each key is then finished as
+// insert_one_t1 does.
+template <class P, int B, int U, class Load>
+__device__ __forceinline__ void insert_t1_many(P* tab, int sp, unsigned first, unsigned stride, unsigned count,
+                                               const Load& load, unsigned& ins, unsigned& maxd, bool& fail) {
+  using K = typename PairTraits<P>::K;
+  using V = typename PairTraits<P>::V;
+  K key[U], ek[U];
+  V val[U], ev[U];
+  uint32_t h[U];
+  bool act[U], ok[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const unsigned i = first + u * stride;
+    act[u] = i < count;
+    if (act[u]) {
+      load(i, key[u], val[u]);
+      act[u] = key[u] != PairTraits<P>::EMPTY && key[u] != PairTraits<P>::TOMB;
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    ok[u] = false;
+    if (act[u]) {
+      h[u] = home_slot(key[u], sp);
+      ek[u] = PairTraits<P>::EMPTY;
+      ev[u] = 0;
+      ok[u] = cas_pair(tab + h[u], ek[u], ev[u], key[u], val[u]);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    if (!act[u]) continue;
+    if (ok[u]) {
+      ++ins;
+      maxd = maxd > 1u ? maxd : 1u;
+    } else {
+      insert_t1_after_cas<P, B>(tab, sp, key[u], val[u], h[u], ek[u], ev[u], ins, maxd, fail);
+    }
   }
 }
 
