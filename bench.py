@@ -1010,9 +1010,12 @@ def run_ours(args):
         bounds = [(c * n // chunks, (c + 1) * n // chunks) for c in range(chunks)]
         step_no = [0]
 
+        marks = []  # per step: compute stream at the step's start, after its first upload wait, at its end
+
         def e2e_step():
             k = step_no[0] % nsets
             step_no[0] += 1
+            mk = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
             bk, bv, bq, bo = bufs[k]
             kv_ready, q_ready = [], []
             with torch.cuda.stream(h2d):
@@ -1029,9 +1032,12 @@ def run_ours(args):
                     ev = torch.cuda.Event()
                     ev.record(h2d)
                     q_ready.append(ev)
+            mk[0].record(stream)
             m.clear(stream=stream)
-            for (a, b), ev in zip(bounds, kv_ready):
+            for c, ((a, b), ev) in enumerate(zip(bounds, kv_ready)):
                 stream.wait_event(ev)
+                if c == 0:
+                    mk[1].record(stream)
                 m.insert(bk[a:b], bv[a:b], target_lf=0.5, stream=stream)
             done = []
             for (a, b), ev in zip(bounds, q_ready):
@@ -1040,6 +1046,8 @@ def run_ours(args):
                 ev2 = torch.cuda.Event()
                 ev2.record(stream)
                 done.append(ev2)
+            mk[2].record(stream)
+            marks.append(mk)
             with torch.cuda.stream(d2h):
                 for (a, b), ev in zip(bounds, done):
                     d2h.wait_event(ev)
@@ -1077,6 +1085,16 @@ def run_ours(args):
         s1.record(stream)
         torch.cuda.synchronize()
         e_el = max_over_ranks(s0.elapsed_time(s1) / 1e3, dev)
+        # where the pipeline's time went, from the compute stream's marks of the timed steps: the
+        # stream's time per step (kernels plus any wait for the first upload), the part of it spent
+        # waiting for that upload (beyond the clear), and the idle gap between steps (the host enqueuing
+        # late)
+        tm = marks[-args.steps:]
+        pipe = {"compute_stream_ms_per_step": round(float(np.mean([x[0].elapsed_time(x[2]) for x in tm])), 3),
+                "upload_wait_ms_per_step": round(max(0.0, float(np.mean([x[0].elapsed_time(x[1]) for x in tm]))
+                                                     - t_clear * 1e3), 3),
+                "host_gap_ms_per_step": round(float(np.mean([tm[i][2].elapsed_time(tm[i + 1][0])
+                                                             for i in range(len(tm) - 1)])) if len(tm) > 1 else 0.0, 3)}
         # the e2e results (the last step's, on the host) equal the exact expectation
         checks["e2e_exact"] = bool(np.array_equal(h_out.numpy().view(np.uint32), expect))
         e2e = {"value": round(world * 2 * n * args.steps / e_el / 1e6, 3), "unit": "Mkeys/s",
@@ -1085,6 +1103,7 @@ def run_ours(args):
                "api": "hashinator_gb300.Hashmap (libhx C ABI); upload, compute and download streams overlapped "
                       f"across steps with {nsets} device buffer sets",
                "host_link": link,
+               "pipeline": pipe,
                "link_bound_ms_per_step": round(3 * n * width / (link["h2d_GB_s"] * 1e9) * 1e3
                                                + n * width / (link["d2h_GB_s"] * 1e9) * 1e3, 3)}
 
