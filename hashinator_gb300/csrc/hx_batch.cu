@@ -174,8 +174,17 @@ __global__ void __launch_bounds__(BLOCK, HX_BATCH_MIN_WARPS * 32 / BLOCK > 0 ? H
             }
           };
           const unsigned cnt = (unsigned)count;
-          for (unsigned base = 0; base < cnt; base += BLOCK * UI)
-            insert_t1_many<P, BT, UI>(tab, sp, base + threadIdx.x, BLOCK, cnt, load, ins, maxd, fail);
+          if (src) {  // moved keys, whose homes are mostly taken: window first, as the single-map clean
+            for (unsigned k = threadIdx.x; k < cnt; k += BLOCK) {
+              K key;
+              V val;
+              load(k, key, val);
+              insert_one_t1_win<P, BT>(tab, sp, key, val, ins, maxd, fail);
+            }
+          } else {
+            for (unsigned base = 0; base < cnt; base += BLOCK * UI)
+              insert_t1_many<P, BT, UI>(tab, sp, base + threadIdx.x, BLOCK, cnt, load, ins, maxd, fail);
+          }
           break;
         }
         case BP_QUERY:

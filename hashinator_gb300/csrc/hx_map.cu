@@ -536,8 +536,13 @@ static hx_status launch_insert(hx_map* m, const void* keys, const void* vals, co
   using K = typename PairTraits<P>::K;
   using V = typename PairTraits<P>::V;
   // clean_tombstones re-inserts its moved keys (count on the device) into a
-  // table whose fill bound still counts the erased keys: thread-per-key
+  // table whose fill bound still counts the erased keys: thread-per-key, and
+  // reading the window before any CAS. A moved key left its home because the
+  // home was taken, and mostly still is, so a blind first CAS at home would
+  // mostly fail: window-first took clean on 2^27 buckets from 0.91 to 0.75 ms
+  // (u32, LF 0.5), 2.05 to 1.62 ms (u32, LF 0.9) and 1.43 to 1.18 ms (u64, LF 0.5).
   const Policy pol = (d_n && m->tune.group == 0) ? Policy{1, 1} : policy(m, Op::INSERT);
+  const bool blind = d_n ? false : m->tune.blind;
   const Geo geo = pick_geo(m, pol.G);
   const int block = m->tune.block;
   if (geo.G == 1) {
@@ -558,7 +563,7 @@ static hx_status launch_insert(hx_map* m, const void* keys, const void* vals, co
   }
 #define HX_LAUNCH_INSERT_T1(PP, BB, UU)                   \
   {                                                       \
-    if (m->tune.blind) HX_LAUNCH_INSERT_T1_B(PP, BB, UU, true) \
+    if (blind) HX_LAUNCH_INSERT_T1_B(PP, BB, UU, true)    \
     else HX_LAUNCH_INSERT_T1_B(PP, BB, UU, false)         \
   }
     HX_T1_DISPATCH(P, nslots(m), U, m->tune.wide, HX_LAUNCH_INSERT_T1);

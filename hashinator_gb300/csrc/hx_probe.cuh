@@ -514,6 +514,26 @@ __device__ __forceinline__ void insert_one_t1(P* tab, int sp, typename PairTrait
   insert_t1_after_cas<P, B>(tab, sp, key, val, h, ek, ev, ins, maxd, fail);
 }
 
+// One key into one table, thread-per-key, reading the home window before any
+// CAS: for keys whose home is probably taken (clean_tombstones' moved keys).
+template <class P, int B>
+__device__ __forceinline__ void insert_one_t1_win(P* tab, int sp, typename PairTraits<P>::K key,
+                                                  typename PairTraits<P>::V val, unsigned& ins, unsigned& maxd,
+                                                  bool& fail) {
+  if (key == PairTraits<P>::EMPTY || key == PairTraits<P>::TOMB) return;
+  const uint32_t h = home_slot(key, sp);
+  Window<P, B> w;
+  load_buckets<B>(tab + (h & ~(uint32_t)(B - 1)), w.k, w.v);
+  unsigned d1 = 0;
+  const int r = insert_t1_win<P, B>(tab, sp, key, val, h, w, d1);
+  if (r == PR_INSERTED) {
+    ++ins;
+    maxd = d1 > maxd ? d1 : maxd;
+  } else if (r == PR_FAIL) {
+    fail = true;
+  }
+}
+
 // U keys per thread, elements first + u * stride (those below count), each
 // loaded by load(i, key, val): their first CASes at home are issued together,
 // so U atomics are in flight per thread, and each key is then finished as
