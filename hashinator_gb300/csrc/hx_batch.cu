@@ -103,8 +103,8 @@ template <class P, int G, int BLOCK>
 #define HX_BATCH_MIN_WARPS 48
 #endif
 // Inserts per thread whose first CAS is in flight at once. One key at a time
-// measured fastest: 4 in flight took the round from 3.12 to 3.57 ms on GB300,
-// the extra live state spilling under the 48-warp register cap.
+// measured fastest on GB300 (2.99 ms a round): 2 in flight at 48 warps per SM
+// took 3.13 ms, 2 or 4 at 32 warps 3.34 / 3.41 ms.
 #ifndef HX_BATCH_INSERTS_IN_FLIGHT
 #define HX_BATCH_INSERTS_IN_FLIGHT 1
 #endif
