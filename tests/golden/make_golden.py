@@ -114,7 +114,7 @@ def make_duplicates() -> None:
     print(f"u32_duplicates: size={res['size_after_insert']}")
 
 
-# ---- operation sequences (the driver's op-script mode) ----------------------
+# ---- operation sequences (ref_driver's op-script mode) ----------------------
 OP_INSERT, OP_QUERY, OP_ERASE, OP_RESIZE, OP_DUMP = 1, 2, 3, 4, 5
 
 
