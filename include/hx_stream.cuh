@@ -119,6 +119,9 @@ __device__ __forceinline__ unsigned warp_incl_scan(unsigned x, int lane) {
 #ifndef HX_STREAM_DEFER
 #define HX_STREAM_DEFER 1
 #endif
+#ifndef HX_STREAM_LANE_CHUNKS
+#define HX_STREAM_LANE_CHUNKS 0  // compaction: each lane owns kR consecutive uint4s (see the kernel)
+#endif
 #ifndef HX_STREAM_MINB
 #define HX_STREAM_MINB 1  // CTAs per SM the register allocation must allow
 #endif
@@ -127,6 +130,7 @@ static_assert(kBlock % 32 == 0 && kBlock <= 1024, "whole warps, at most 32 of th
 constexpr int kR = HX_STREAM_R;
 constexpr int kStages = HX_STREAM_STAGES;
 constexpr int kDefer = HX_STREAM_DEFER;
+constexpr bool kLaneChunks = HX_STREAM_LANE_CHUNKS != 0;
 static_assert(kDefer >= 1 && kDefer < kStages, "a stage must be free to load while D phases wait");
 // Count slots per CTA. In phase p a CTA publishes its count of p, then
 // reads every CTA's count of p - D; so when it publishes p it has read every
@@ -298,9 +302,19 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
       T x[kR][E];
       uint4* stage = s_stage + (size_t)st * SU4;
       const unsigned wbase = warp * 32 * kR;  // this warp's first uint4 of the slice
+      // Where register row r comes from. By default row r of the warp is 32
+      // consecutive uint4s, one per lane. With lane chunks (compaction only),
+      // lane l owns the kR consecutive uint4s l*kR .. l*kR+kR-1 of the warp's
+      // part and row r holds its uint4 (r + l) mod kR: rotated, so that the 8
+      // lanes of a shared-memory wavefront read 8 different bank groups.
+      constexpr bool LANE = kLaneChunks && !SCAN && (kR & (kR - 1)) == 0 && kR * E <= 32;
+      auto u_of = [&](int r) -> unsigned {
+        if constexpr (LANE) return wbase + lane * kR + ((r + lane) & (kR - 1));
+        else return wbase + r * 32 + lane;
+      };
 #pragma unroll
       for (int r = 0; r < kR; ++r) {
-        const unsigned u = wbase + r * 32 + lane;
+        const unsigned u = u_of(r);
         if (whole) {
           const uint4 q = stage[u];
           memcpy(&x[r][0], &q, 16);
@@ -321,6 +335,7 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
       unsigned acc = 0;
       unsigned bits[kR];
       unsigned cnt[kR];
+      unsigned lm = 0;  // lane chunks: the lane's selections, bit j*E + q for element q of its uint4 j
 #pragma unroll
       for (int r = 0; r < kR; ++r) {
         unsigned c;
@@ -328,7 +343,7 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
           c = x[r][0] + x[r][1] + x[r][2] + x[r][3];
           bits[r] = 0;
         } else {
-          const uint64_t e = e0 + (uint64_t)(wbase + r * 32 + lane) * E;
+          const uint64_t e = e0 + (uint64_t)u_of(r) * E;
           unsigned m = 0;
           if (whole) {  // block-uniform: no per-element bounds checks in a whole slice
 #pragma unroll
@@ -355,6 +370,7 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
             }
           }
           bits[r] = m;
+          if constexpr (LANE) lm |= m << (((r + lane) & (kR - 1)) * E);
           c = __popc(m);
         }
         cnt[r] = c;
@@ -364,7 +380,13 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
           acc += __shfl_sync(0xffffffffu, incl, 31);
         }
       }
-      if constexpr (!SCAN) {
+      unsigned lane_pre = 0;  // lane chunks: selections of the warp's lanes before this one
+      if constexpr (LANE) {
+        const unsigned c = __popc(lm);
+        const unsigned incl = warp_incl_scan(c, lane);
+        lane_pre = incl - c;
+        acc = __shfl_sync(0xffffffffu, incl, 31);
+      } else if constexpr (!SCAN) {
         // Ranks of the selections: a lane's count per uint4 is at most 4 and a
         // warp's sum at most 128, so four uint4s share one 32-bit word as byte
         // lanes with no carries between them: one warp scan per four uint4s.
@@ -412,7 +434,13 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
 #pragma unroll
         for (int r = 0; r < kR; ++r) {
           if (!bits[r]) continue;  // nothing selected in this uint4: the common case for a sparse rule
-          unsigned o = woff + pre[r];
+          unsigned o;
+          if constexpr (LANE) {
+            const unsigned jb = ((r + lane) & (kR - 1)) * E;  // first bit of this uint4 in the lane's mask
+            o = woff + lane_pre + __popc(lm & ((1u << jb) - 1u));
+          } else {
+            o = woff + pre[r];
+          }
 #pragma unroll
           for (int q = 0; q < E; ++q)
             if (bits[r] & (1u << q)) packed[o++] = hxs::project<T, O>(x[r][q]);
