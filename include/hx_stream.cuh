@@ -305,8 +305,9 @@ __global__ void __launch_bounds__(kBlock, HX_STREAM_MINB) k_stream(const T* __re
       // Where register row r comes from. By default row r of the warp is 32
       // consecutive uint4s, one per lane. With lane chunks (compaction only),
       // lane l owns the kR consecutive uint4s l*kR .. l*kR+kR-1 of the warp's
-      // part and row r holds its uint4 (r + l) mod kR: rotated, so that the 8
-      // lanes of a shared-memory wavefront read 8 different bank groups.
+      // part and row r holds its uint4 (r + l) mod kR: rotated, so that with
+      // kR = 8 the 8 lanes of a shared-memory wavefront read 8 different bank
+      // groups.
       constexpr bool LANE = kLaneChunks && !SCAN && (kR & (kR - 1)) == 0 && kR * E <= 32;
       auto u_of = [&](int r) -> unsigned {
         if constexpr (LANE) return wbase + lane * kR + ((r + lane) & (kR - 1));
