@@ -994,13 +994,15 @@ def run_ours(args):
         h_vals = torch.from_numpy(vals.view(np.int32)).pin_memory()
         h_q = torch.from_numpy(q.view(np.int32)).pin_memory()
         h_out = torch.empty(n, dtype=torch.int32).pin_memory()
-        # Several device buffer sets and separate upload / download streams: later
-        # steps' uploads run while step k's kernels do; a set is reused only after the
-        # step that last used it has consumed its inputs and downloaded its results.
-        # With two sets, step k's uploads wait for step k-2's downloads and end just
-        # as step k-1's kernels do; a third set takes that wait off the path.
+        # Several device buffer sets, rotated; a set is reused only after the step that
+        # last used it has consumed its inputs and downloaded its results. Two copy
+        # streams (--e2e-copy-streams 2): uploads and downloads on their own streams,
+        # step k+1's uploads running while step k's kernels do. One copy stream (1):
+        # every copy in one order, step k+1's uploads queued before step k's downloads,
+        # so the host link carries one direction at a time.
+        one_copy = args.e2e_copy_streams == 1
         h2d = torch.cuda.Stream(device=dev)
-        d2h = torch.cuda.Stream(device=dev)
+        d2h = h2d if one_copy else torch.cuda.Stream(device=dev)
         nsets = max(2, args.e2e_sets)
         bufs = [(d_keys, d_vals, d_q, d_out)] + [
             (torch.empty_like(d_keys), torch.empty_like(d_vals), torch.empty_like(d_q), d_out.clone())
@@ -1012,11 +1014,9 @@ def run_ours(args):
 
         marks = []  # per step: compute stream at the step's start, after its first upload wait, at its end
 
-        def e2e_step():
-            k = step_no[0] % nsets
-            step_no[0] += 1
-            mk = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-            bk, bv, bq, bo = bufs[k]
+        def upload(i):
+            k = i % nsets
+            bk, bv, bq, _ = bufs[k]
             kv_ready, q_ready = [], []
             with torch.cuda.stream(h2d):
                 if free[k] is not None:
@@ -1032,6 +1032,13 @@ def run_ours(args):
                     ev = torch.cuda.Event()
                     ev.record(h2d)
                     q_ready.append(ev)
+            return kv_ready, q_ready
+
+        def compute_and_download(i, ready):
+            k = i % nsets
+            kv_ready, q_ready = ready
+            mk = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            bk, bv, bq, bo = bufs[k]
             mk[0].record(stream)
             m.clear(stream=stream)
             for c, ((a, b), ev) in enumerate(zip(bounds, kv_ready)):
@@ -1056,8 +1063,17 @@ def run_ours(args):
             fin.record(d2h)  # after every kernel of this step (waited on) and its downloads
             free[k] = fin
 
-        for _ in range(max(1, args.warmup // 2)):
-            e2e_step()
+        def e2e_steps(count):
+            """count steps; each step's uploads are queued one step ahead of its kernels."""
+            first = step_no[0]
+            ready = upload(first)
+            for i in range(first, first + count):
+                nxt = upload(i + 1) if i + 1 < first + count else None
+                compute_and_download(i, ready)
+                ready = nxt
+            step_no[0] = first + count
+
+        e2e_steps(max(1, args.warmup // 2))
         torch.cuda.synchronize()
         # the host link alone: one step's uploads and downloads as plain pinned copies, best of 3
         link = {}
@@ -1079,8 +1095,7 @@ def run_ours(args):
         s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s0.record(stream)
         h2d.wait_event(s0)  # the first uploads start inside the timed region
-        for _ in range(args.steps):
-            e2e_step()
+        e2e_steps(args.steps)
         stream.wait_event(free[(step_no[0] - 1) % nsets])  # the timed region ends with the last results on the host
         s1.record(stream)
         torch.cuda.synchronize()
@@ -1100,8 +1115,8 @@ def run_ours(args):
         e2e = {"value": round(world * 2 * n * args.steps / e_el / 1e6, 3), "unit": "Mkeys/s",
                "h2d_bytes_per_step": 3 * n * width, "d2h_bytes_per_step": n * width,
                "ms_per_step": round(e_el / args.steps * 1e3, 3), "chunks": chunks,
-               "api": "hashinator_gb300.Hashmap (libhx C ABI); upload, compute and download streams overlapped "
-                      f"across steps with {nsets} device buffer sets",
+               "api": "hashinator_gb300.Hashmap (libhx C ABI); copies overlapped with the kernels across steps, "
+                      f"{nsets} device buffer sets, {args.e2e_copy_streams} copy stream(s)",
                "host_link": link,
                "pipeline": pipe,
                "link_bound_ms_per_step": round(3 * n * width / (link["h2d_GB_s"] * 1e9) * 1e3
@@ -1275,6 +1290,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-chunks", type=int, default=2)
     ap.add_argument("--e2e-sets", type=int, default=3, help="device buffer sets the e2e pipeline rotates")
+    ap.add_argument("--e2e-copy-streams", type=int, default=1, choices=[1, 2],
+                    help="1: one copy stream, one direction at a time; 2: uploads and downloads on their own streams")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-maps", type=int, default=4096)
     ap.add_argument("--batched-tuning", type=int, nargs=3, metavar=("GROUP", "BLOCK", "TILE"),
