@@ -1012,7 +1012,14 @@ def run_ours(args):
         bounds = [(c * n // chunks, (c + 1) * n // chunks) for c in range(chunks)]
         step_no = [0]
 
-        marks = []  # per step: compute stream at the step's start, after its first upload wait, at its end
+        marks = []  # per step: the compute stream at the step's start and at its end
+        waits = []  # per step: (before, after) each wait of the compute stream on an upload
+        up_spans = []  # per step: the copy stream at the start and the end of its uploads
+
+        def timing_event(s_):
+            e_ = torch.cuda.Event(enable_timing=True)
+            e_.record(s_)
+            return e_
 
         def upload(i):
             k = i % nsets
@@ -1021,6 +1028,7 @@ def run_ours(args):
             with torch.cuda.stream(h2d):
                 if free[k] is not None:
                     h2d.wait_event(free[k])
+                u0 = timing_event(h2d)
                 for a, b in bounds:
                     bk[a:b].copy_(h_keys[a:b], non_blocking=True)
                     bv[a:b].copy_(h_vals[a:b], non_blocking=True)
@@ -1032,29 +1040,34 @@ def run_ours(args):
                     ev = torch.cuda.Event()
                     ev.record(h2d)
                     q_ready.append(ev)
+                up_spans.append((u0, timing_event(h2d)))
             return kv_ready, q_ready
 
         def compute_and_download(i, ready):
             k = i % nsets
             kv_ready, q_ready = ready
-            mk = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            mk = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
             bk, bv, bq, bo = bufs[k]
+            wl = []
             mk[0].record(stream)
             m.clear(stream=stream)
-            for c, ((a, b), ev) in enumerate(zip(bounds, kv_ready)):
+            for (a, b), ev in zip(bounds, kv_ready):
+                w0 = timing_event(stream)
                 stream.wait_event(ev)
-                if c == 0:
-                    mk[1].record(stream)
+                wl.append((w0, timing_event(stream)))
                 m.insert(bk[a:b], bv[a:b], target_lf=0.5, stream=stream)
             done = []
             for (a, b), ev in zip(bounds, q_ready):
+                w0 = timing_event(stream)
                 stream.wait_event(ev)
+                wl.append((w0, timing_event(stream)))
                 m.retrieve(bq[a:b], bo[a:b], stream=stream)
                 ev2 = torch.cuda.Event()
                 ev2.record(stream)
                 done.append(ev2)
-            mk[2].record(stream)
+            mk[1].record(stream)
             marks.append(mk)
+            waits.append(wl)
             with torch.cuda.stream(d2h):
                 for (a, b), ev in zip(bounds, done):
                     d2h.wait_event(ev)
@@ -1100,15 +1113,20 @@ def run_ours(args):
         s1.record(stream)
         torch.cuda.synchronize()
         e_el = max_over_ranks(s0.elapsed_time(s1) / 1e3, dev)
-        # where the pipeline's time went, from the compute stream's marks of the timed steps: the
-        # stream's time per step (kernels plus any wait for the first upload), the part of it spent
-        # waiting for that upload (beyond the clear), and the idle gap between steps (the host enqueuing
-        # late)
+        # where the pipeline's time went, from events on the compute and copy streams over the timed
+        # steps: the compute stream's time per step, the part of it spent waiting for uploads, the rest
+        # (kernels), the upload rate the copy stream achieved while kernels ran, and the idle gap between
+        # steps (the host enqueuing late)
         tm = marks[-args.steps:]
-        pipe = {"compute_stream_ms_per_step": round(float(np.mean([x[0].elapsed_time(x[2]) for x in tm])), 3),
-                "upload_wait_ms_per_step": round(max(0.0, float(np.mean([x[0].elapsed_time(x[1]) for x in tm]))
-                                                     - t_clear * 1e3), 3),
-                "host_gap_ms_per_step": round(float(np.mean([tm[i][2].elapsed_time(tm[i + 1][0])
+        tw = waits[-args.steps:]
+        t_stream = float(np.mean([x[0].elapsed_time(x[1]) for x in tm]))
+        t_wait = float(np.mean([sum(a.elapsed_time(b) for a, b in wl) for wl in tw]))
+        t_up = float(np.median([a.elapsed_time(b) for a, b in up_spans[-args.steps:]]))
+        pipe = {"compute_stream_ms_per_step": round(t_stream, 3),
+                "upload_wait_ms_per_step": round(t_wait, 3),
+                "kernels_ms_per_step": round(t_stream - t_wait, 3),
+                "h2d_GB_s_in_pipeline": round(3 * n * width / (t_up * 1e-3) / 1e9, 1),
+                "host_gap_ms_per_step": round(float(np.mean([tm[i][1].elapsed_time(tm[i + 1][0])
                                                              for i in range(len(tm) - 1)])) if len(tm) > 1 else 0.0, 3)}
         # the e2e results (the last step's, on the host) equal the exact expectation
         checks["e2e_exact"] = bool(np.array_equal(h_out.numpy().view(np.uint32), expect))
