@@ -1015,6 +1015,7 @@ def run_ours(args):
         marks = []  # per step: the compute stream at the step's start and at its end
         waits = []  # per step: (before, after) each wait of the compute stream on an upload
         up_spans = []  # per step: the copy stream at the start and the end of its uploads
+        down_spans = []  # per step: (start, end) of each download, each start after its wait
 
         def timing_event(s_):
             e_ = torch.cuda.Event(enable_timing=True)
@@ -1069,9 +1070,13 @@ def run_ours(args):
             marks.append(mk)
             waits.append(wl)
             with torch.cuda.stream(d2h):
+                dl = []
                 for (a, b), ev in zip(bounds, done):
                     d2h.wait_event(ev)
+                    d0 = timing_event(d2h)
                     h_out[a:b].copy_(bo[a:b], non_blocking=True)
+                    dl.append((d0, timing_event(d2h)))
+                down_spans.append(dl)
             fin = torch.cuda.Event()
             fin.record(d2h)  # after every kernel of this step (waited on) and its downloads
             free[k] = fin
@@ -1122,10 +1127,12 @@ def run_ours(args):
         t_stream = float(np.mean([x[0].elapsed_time(x[1]) for x in tm]))
         t_wait = float(np.mean([sum(a.elapsed_time(b) for a, b in wl) for wl in tw]))
         t_up = float(np.median([a.elapsed_time(b) for a, b in up_spans[-args.steps:]]))
+        t_down = float(np.median([sum(a.elapsed_time(b) for a, b in dl) for dl in down_spans[-args.steps:]]))
         pipe = {"compute_stream_ms_per_step": round(t_stream, 3),
                 "upload_wait_ms_per_step": round(t_wait, 3),
                 "kernels_ms_per_step": round(t_stream - t_wait, 3),
                 "h2d_GB_s_in_pipeline": round(3 * n * width / (t_up * 1e-3) / 1e9, 1),
+                "d2h_GB_s_in_pipeline": round(n * width / (t_down * 1e-3) / 1e9, 1),
                 "host_gap_ms_per_step": round(float(np.mean([tm[i][1].elapsed_time(tm[i + 1][0])
                                                              for i in range(len(tm) - 1)])) if len(tm) > 1 else 0.0, 3)}
         # the e2e results (the last step's, on the host) equal the exact expectation
