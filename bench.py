@@ -1315,8 +1315,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-chunks", type=int, default=2)
     ap.add_argument("--e2e-sets", type=int, default=3, help="device buffer sets the e2e pipeline rotates")
-    ap.add_argument("--e2e-copy-streams", type=int, default=1, choices=[1, 2],
-                    help="1: one copy stream, one direction at a time; 2: uploads and downloads on their own streams")
+    ap.add_argument("--e2e-copy-streams", type=int, default=2, choices=[1, 2],
+                    help="2: uploads and downloads on their own streams; 1: one copy stream, one direction at a time")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-maps", type=int, default=4096)
     ap.add_argument("--batched-tuning", type=int, nargs=3, metavar=("GROUP", "BLOCK", "TILE"),
