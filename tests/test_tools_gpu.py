@@ -121,9 +121,9 @@ def test_copy_if_capacity_and_device_count(hx, oracle_mod):
 @pytest.mark.parametrize("eb", [4, 8, 16])
 @pytest.mark.parametrize("off", [0, 4, 8, 12])
 def test_copy_if_output_offsets_and_capacity_cuts(hx, eb, off):
-    """The compaction stores each CTA's run with 16-byte stores between
-    element-by-element edges: outputs that start 4, 8 or 12 bytes past a
-    16-byte boundary, and capacities that cut a run anywhere. The bytes before
+    """Outputs that start 4, 8 or 12 bytes past a 16-byte boundary, and
+    capacities that cut a CTA's run of output anywhere (each CTA writes its
+    selections at an offset that no alignment constrains). The bytes before
     the output and after the last stored element stay as they were. An output
     that is not a multiple of the element size from 16-byte alignment (8-byte
     pairs at 4 bytes, 16-byte pairs at 4, 8, 12) is rejected before any
